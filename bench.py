@@ -1,0 +1,405 @@
+"""Benchmark: batched transient-CW F-statistic maps on GB300.
+
+Workload (N=1): 4096 templates, SFT counts uniform in 200..4000 with 0-30 %
+of SFTs dropped as gaps, half rectangular and half exponential windows,
+(t0, tau) grid sizes uniform in 256..2048 per axis -- about 5.4e9 cells per
+step -- synthetic seeded atoms (pyfstat_gb300.synth).  A step is one pass of
+the batched fused path over all templates (prefix kernel, persistent map
+kernel, finalize kernel; one CUDA graph), giving max2F, argmax and FP64
+lnBtSG per template.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  Under torchrun each rank runs its own 4096 templates
+(weak scaling, no collective on the data path); rank 0 prints.
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = ("2F-map cells/s, batched+fused vs plain per-template kernel, "
+          "2F rel err ≤1e-5")
+UNIT = "cells/s"
+# Algorithmic per-cell work of the transient map (reference per-cell math,
+# compensation not counted): FP32 flops (an FMA counts 2) and MUFU ops.
+FLOPS_PER_CELL = {1: 34.0, 2: 55.0}
+MUFU_PER_CELL = 3.0
+TRAFFIC_FILE = os.path.join(REPO, "profiles", "map_kernel_batched4096.md")
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--templates", type=int, default=4096)
+    p.add_argument("--seed", type=int, default=12345)
+    p.add_argument("--cpu-seconds", type=float, default=12.0,
+                   help="target CPU time of the bounded CPU-baseline sample")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--plain-templates", type=int, default=256,
+                   help="templates timed with the plain per-template kernel")
+    p.add_argument("--tile", type=str, default="",
+                   help="tile config as JSON, 'auto' for the autotuner, empty for defaults")
+    return p.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def workload(n_templates, seed):
+    from pyfstat_gb300 import synth
+
+    return synth.batched_templates(n_templates, seed=seed)
+
+
+# ------------------------------------------------------------------ clocks
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+
+    FIELDS = ("uuid,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, uuid=None):
+        self.uuid = uuid
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        rows = []
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) != 9:
+                continue
+            if self.uuid and parts[0] != self.uuid:
+                continue
+            rows.append(parts)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def gpu_uuid(torch, dev):
+    try:
+        u = str(torch.cuda.get_device_properties(dev).uuid)
+        return u if u.startswith("GPU-") else "GPU-" + u
+    except Exception:
+        return None
+
+
+# ------------------------------------------------------------------ CPU baseline
+
+
+def cpu_baseline(templates, seconds, threads):
+    """The reference's per-template CPU path restated in C (oracle port: the
+    pycuda kernels' FP32 arithmetic, OpenMP over rows/cells) plus its numpy
+    max/argmax/lnBtSG, over consecutive templates until ~`seconds`."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+    from pyfstat_gb300.batched import template_grids
+
+    O.build()
+    cells, used = 0, 0
+    t0 = time.perf_counter()
+    for t in templates:
+        t0s, taus = template_grids(t)
+        fn = O.rect_map_f32 if t["window"] == 1 else O.exp_map_f32
+        F = fn(t["atoms"], t["TAtom"], t["t0_data"], t0s, taus, nthreads=threads)
+        O.max_argmax(F)
+        O.lnBtSG(F)
+        cells += F.size
+        used += 1
+        if time.perf_counter() - t0 > seconds and used >= 2:
+            break
+    dt = time.perf_counter() - t0
+    return cells / dt, cells, used, dt
+
+
+def traffic_per_launch():
+    """DRAM bytes per map-kernel launch from the committed ncu summary, if any."""
+    try:
+        with open(TRAFFIC_FILE) as f:
+            for line in f:
+                if line.strip().startswith("traffic_bytes_per_launch"):
+                    return float(line.split("=")[1].split()[0])
+    except (OSError, ValueError, IndexError):
+        pass
+    return None
+
+
+# ------------------------------------------------------------------ arms
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    templates = workload(args.templates, args.seed)
+    for _ in range(args.warmup):
+        cpu_baseline(templates, min(2.0, args.cpu_seconds), threads)
+    vals, samples = [], []
+    t_all = time.perf_counter()
+    for _ in range(args.steps):
+        v, cells, used, dt = cpu_baseline(templates, args.cpu_seconds, threads)
+        vals.append(v)
+        samples.append((cells, used, dt))
+    elapsed = time.perf_counter() - t_all
+    value = float(statistics.median(vals))
+    cells, used, dt = samples[-1]
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"batched {args.templates} templates, rect+exp, "
+                   "SFTs 200-4000, 0-30% gaps, grids 256-2048^2",
+                   "sample": "consecutive templates per step (bounded CPU time)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{used} templates, {cells} cells, {dt:.1f} s per step"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, ws, rank, local):
+    import torch
+
+    from pyfstat_gb300 import _lib
+    from pyfstat_gb300.batched import TransientMapBatch, template_grids
+
+    if ws > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local if ws > 1 else 0)
+    torch.cuda.set_device(dev)
+
+    templates = workload(args.templates, args.seed + 1000003 * rank)
+    tile = None
+    if args.tile == "auto":
+        tile = "auto"
+    elif args.tile:
+        tile = json.loads(args.tile)
+    batch = TransientMapBatch(templates, device=dev.index, tile_config=tile)
+    h = batch.handle
+    stream = torch.cuda.current_stream(dev)
+    h.set_stream(stream.cuda_stream)
+    n_cells = batch.n_cells
+    n_t = batch.n_templates
+    d_atoms = torch.from_numpy(batch.atoms).to(dev)
+    d_res = torch.zeros(n_t * 5, dtype=torch.float64, device=dev)
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if ws > 1:
+            torch.distributed.barrier()
+
+    for _ in range(max(3, args.warmup)):
+        batch.run_device(d_atoms, d_res, use_graph=True)
+    barrier()
+    clocks = ClockSampler(gpu_uuid(torch, dev))
+    clocks.start()
+    time.sleep(0.3)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    barrier()
+    e0.record(stream)
+    for _ in range(args.steps):
+        batch.run_device(d_atoms, d_res, use_graph=True)
+    e1.record(stream)
+    barrier()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    if ws > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = n_cells * ws / (ms * 1e-3)
+    res = d_res.cpu().numpy().view(_lib.RESULT_DTYPE)
+    assert np.all(np.isfinite(res["lnBtSG"])) and np.all(res["maxF"] > 0)
+
+    # per-kernel durations (events between the launches, same stream)
+    kms = np.array([batch.plan.run_timed(d_atoms, d_res) for _ in range(args.steps)])
+    prefix_ms, map_ms, fin_ms = (float(x) for x in kms.mean(axis=0))
+
+    # end to end through the public API with pinned host buffers
+    pinned = torch.empty(batch.atoms.shape, dtype=torch.float32, pin_memory=True)
+    pinned.numpy()[:] = batch.atoms
+    host_atoms = pinned.numpy()
+    batch.run(host_atoms)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        out = batch.run(host_atoms)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if ws > 1:
+        t = torch.tensor([e2e_s], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    assert np.array_equal(out["argmax"], res["argmax"])
+
+    # plain per-template kernel (map written, one call per template) on a subset
+    plain = None
+    if rank == 0 and args.plain_templates > 0:
+        sub = templates[:args.plain_templates]
+        maxcells = max(int(t["N_t0"]) * int(t["N_tau"]) for t in sub)
+        d_map = torch.empty(maxcells, dtype=torch.float32, device=dev)
+        d_r1 = torch.zeros(5, dtype=torch.float64, device=dev)
+        dev_t = []
+        for t in sub:
+            t0s, taus = template_grids(t)
+            dev_t.append((torch.from_numpy(t["atoms"]).to(dev),
+                          torch.from_numpy(t0s.view(np.int32)).to(dev),
+                          torch.from_numpy(taus.view(np.int32)).to(dev), t))
+        def plain_pass():
+            for A, t0s, taus, t in dev_t:
+                h.map_plain(A, A.shape[0], t["TAtom"], t["t0_data"], t["window"], t0s,
+                            t0s.shape[0], taus, taus.shape[0], d_map, d_r1,
+                            flags=_lib.TCW_FLAG_LNBTSG)
+        plain_pass()
+        torch.cuda.synchronize(dev)
+        p0 = torch.cuda.Event(enable_timing=True)
+        p1 = torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        plain_pass()
+        p1.record(stream)
+        torch.cuda.synchronize(dev)
+        pcells = sum(int(t["N_t0"]) * int(t["N_tau"]) for t in sub)
+        pval = pcells / (p0.elapsed_time(p1) * 1e-3)
+        plain = {"value": pval, "unit": UNIT, "templates": len(sub),
+                 "ratio_batched_over_plain": value / ws / pval,
+                 "note": "one tcw_map_plain call per template, full F map written"}
+
+    if rank != 0:
+        if ws > 1:
+            torch.distributed.destroy_process_group()
+        return
+
+    peaks = _lib.probe_peaks(dev.index)
+    n_rect = int(np.sum(batch.desc["window"] == 1))
+    cells_w = {w: float(np.sum(batch.desc["N_t0"][batch.desc["window"] == w].astype(np.float64)
+                               * batch.desc["N_tau"][batch.desc["window"] == w]))
+               for w in (1, 2)}
+    flops = sum(cells_w[w] * FLOPS_PER_CELL[w] for w in (1, 2))
+    achieved_tflops = flops / (map_ms * 1e-3) / 1e12
+    mufu_rate = n_cells * MUFU_PER_CELL / (map_ms * 1e-3) / 1e12
+    fp32_frac = achieved_tflops / peaks["fp32_tflops"]
+    mufu_frac = mufu_rate / peaks["mufu_tops"]
+    bound = "fp32" if fp32_frac >= mufu_frac else "mufu"
+    roofline = {
+        "bound": bound,
+        "achieved": achieved_tflops if bound == "fp32" else mufu_rate,
+        "peak": peaks["fp32_tflops"] if bound == "fp32" else peaks["mufu_tops"],
+        "unit": "TFLOP/s" if bound == "fp32" else "Tops/s",
+        "frac": fp32_frac if bound == "fp32" else mufu_frac,
+        "traffic": traffic_per_launch(),
+        "kernel": "map_kernel (persistent, batched)",
+        "kernel_ms": map_ms, "prefix_ms": prefix_ms, "finalize_ms": fin_ms,
+        "peak_source": "measured on this GPU by tcw_probe_peaks (FMA chains / ex2 chains)",
+        "algorithmic": {"fp32_flops_per_cell": FLOPS_PER_CELL, "mufu_per_cell": MUFU_PER_CELL,
+                        "fp32_frac": fp32_frac, "mufu_frac": mufu_frac},
+        "measured_peaks": peaks,
+    }
+    atoms_bytes = batch.atoms.nbytes
+    hbm_peak = None
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            hbm_peak = json.load(f).get("hbm_gbs")
+    except (OSError, ValueError):
+        pass
+    roofline["hbm_view"] = {"algorithmic_bytes_per_launch": atoms_bytes + 40 * n_t,
+                            "achieved_gbs": (atoms_bytes + 40 * n_t) / (map_ms * 1e-3) / 1e9,
+                            "peak_gbs": hbm_peak}
+
+    cpu = None
+    if not args.no_cpu_baseline and ws == 1:
+        threads = os.cpu_count() or 1
+        v, cells, used, dt = cpu_baseline(templates, args.cpu_seconds, threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"first {used} templates ({cells} cells, {dt:.1f} s), oracle port of "
+                         "the reference pycuda kernels' FP32 arithmetic + numpy reductions"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"batched {n_t} templates per GPU ({n_rect} rect, "
+                   f"{n_t - n_rect} exp), SFTs 200-4000 with 0-30% gaps, grids 256-2048 per "
+                   "axis, one CUDA graph per step",
+                   "cells_per_step_per_gpu": n_cells, "atoms_bytes": atoms_bytes,
+                   "l2": "inputs and per-template prefix rows larger than L2",
+                   "tile_config": batch.tile_config, "parallelism": f"templates x{ws} ranks"},
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "e2e": {"value": n_cells * ws / e2e_s, "unit": UNIT, "h2d_bytes_per_step": atoms_bytes,
+                "d2h_bytes_per_step": 40 * n_t,
+                "api": "TransientMapBatch.run (tcw_plan_run_host), pinned host atoms"},
+        "plain_per_template": plain,
+        "gpu_launches": 3 * args.steps,
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        run_ours(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,164 @@
+/*
+ * tcw_b200.h -- C ABI of the GB300 (sm_103a) transient-CW F-statistic map.
+ *
+ * This library is the compute behind a 'b200' version of PyFstat's
+ * transient F-stat map, a drop-in beside the 'lal' and 'pycuda' versions of
+ * pyfstat/tcw_fstat_map_funcs.py (version table at :320-327, dispatcher
+ * call_compute_transient_fstat_map at :495-544).  Its entry points replace
+ * what the pycuda version does per call:
+ *   - the H2D copy of the (numAtoms, 7) atoms matrix        (tcw:864, :945)
+ *   - the rect / exp kernel launch                          (tcw:896-909, :977-991)
+ *   - the D2H copy of the full FP32 map                     (tcw:912, :994)
+ *   - max, argmax, lnBtSG and the t0/tau posteriors on host (tcw:810-828, :196-287)
+ * and add a batched form for many templates in one launch.
+ *
+ * Conventions
+ *   - Every function returns an int status: TCW_OK (0) or a negative
+ *     TCW_ERR_* code; nothing throws or aborts.  tcw_strerror() names a code,
+ *     tcw_last_error() gives the handle's last detailed message.
+ *   - Atoms are row-major (numAtoms, 7) float32 matrices with columns
+ *     [a2, b2, ab, Fa_re, Fa_im, Fb_re, Fb_im] -- the matrix PyFstat builds at
+ *     tcw:711-721 -- on the binned grid t_i = t0_data + i*TAtom.
+ *   - Grids are explicit u32 arrays t0s[N_t0] and taus[N_tau] (seconds); a
+ *     lalpulsar transientWindowRange_t expands to t0 + m*dt0, tau + n*dtau.
+ *     Rectangular maps need a non-decreasing tau grid.
+ *   - The F map is row-major float32 [m][n] (m over t0, n over tau) and
+ *     holds F, not 2F, exactly like pyTransientFstatMap.F_mn.
+ *   - One handle per host thread; calls on a handle are asynchronous on its
+ *     stream unless named *_host (those synchronise before returning).
+ */
+#ifndef TCW_B200_H
+#define TCW_B200_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TCW_ABI_VERSION 1
+
+/* status codes */
+#define TCW_OK 0
+#define TCW_ERR_INVALID_ARG (-1)
+#define TCW_ERR_CUDA (-2)
+#define TCW_ERR_NO_DEVICE (-3)
+#define TCW_ERR_ALLOC (-4)
+#define TCW_ERR_TIMEOUT (-5)
+#define TCW_ERR_UNSUPPORTED (-6)
+#define TCW_ERR_OVERFLOW (-7)
+
+/* window types: lalpulsar's transientWindowType_t values */
+#define TCW_WINDOW_NONE 0
+#define TCW_WINDOW_RECT 1
+#define TCW_WINDOW_EXP 2
+
+/* flags for map calls */
+#define TCW_FLAG_LNBTSG 0x1       /* compute lnBtSG (tcw:196-217) */
+#define TCW_FLAG_POSTERIORS 0x2   /* t0/tau max-posterior indices (tcw:219-287); needs a map */
+#define TCW_FLAG_FP64_DET 0x4     /* determinant D in native FP64 instead of FP32 double-word */
+#define TCW_FLAG_UNCOMPENSATED 0x8 /* plain FP32 sums and D (precision studies only) */
+
+/* Per-map / per-template result. */
+typedef struct {
+  double lnBtSG;      /* ln(70/(N_t0 N_tau)) + ln sum_mn exp(F_mn), FP64 */
+  int64_t argmax;     /* flat index m*N_tau + n of maxF, first occurrence */
+  int64_t t0_mp_idx;  /* argmax_m sum_n exp(F_mn - maxF) (TCW_FLAG_POSTERIORS) */
+  int64_t tau_mp_idx; /* argmax_n sum_m exp(F_mn - maxF) (TCW_FLAG_POSTERIORS) */
+  float maxF;         /* max F (not 2F) */
+  int32_t status;     /* 0 */
+} tcw_result;
+
+/* One template of a batched call. */
+typedef struct {
+  uint64_t atom_offset; /* first row of this template in the concatenated atoms */
+  uint64_t t0_offset;   /* first entry in the concatenated t0 grid */
+  uint64_t tau_offset;  /* first entry in the concatenated tau grid */
+  uint32_t numAtoms;
+  uint32_t TAtom;
+  uint32_t t0_data;
+  int32_t window;       /* TCW_WINDOW_RECT or TCW_WINDOW_EXP */
+  uint32_t N_t0;
+  uint32_t N_tau;
+} tcw_template_desc;
+
+/* Tile shapes of a batched plan (0 = library default / autotuned). */
+typedef struct {
+  uint32_t rect_tn;       /* columns per rect block: 32, 64 or 128 */
+  uint32_t rect_tm;       /* rows per rect tile */
+  uint32_t exp_tn;        /* columns per exp block: 32, 64 or 128 */
+  uint32_t exp_rows;      /* rows per exp thread chunk (0 = whole column) */
+  uint32_t blocks_per_sm; /* persistent blocks per SM */
+} tcw_tile_config;
+
+typedef struct tcw_handle tcw_handle;
+typedef struct tcw_plan tcw_plan;
+
+int tcw_abi_version(void);
+const char *tcw_strerror(int status);
+const char *tcw_last_error(const tcw_handle *h);
+
+/* Device discovery (replaces the pycuda device probing of tcw:419-470). */
+int tcw_device_count(int *count);
+int tcw_device_info(int device, char *name, size_t name_len, int *cc_major, int *cc_minor,
+                    size_t *total_mem);
+
+/* Handle: owns a CUDA stream and a grow-only device workspace on `device`. */
+int tcw_create(tcw_handle **h, int device);
+int tcw_destroy(tcw_handle *h);
+int tcw_get_stream(tcw_handle *h, void **stream);
+int tcw_set_stream(tcw_handle *h, void *stream); /* NULL = the handle's own stream */
+int tcw_sync(tcw_handle *h, int timeout_ms);     /* TCW_ERR_TIMEOUT if not done in time */
+
+/* Plain per-template map on device buffers.  d_Fmn may be NULL (no map is
+ * written; TCW_FLAG_POSTERIORS then needs a map and is rejected).  d_result
+ * is one device tcw_result.  Replaces pycuda_compute_transient_fstat_map
+ * (tcw:656-834) with its rect / exp launches (tcw:837-916, :919-998). */
+int tcw_map_plain(tcw_handle *h, const float *d_atoms, uint32_t numAtoms, uint32_t TAtom,
+                  uint32_t t0_data, int window, const uint32_t *d_t0s, uint32_t N_t0,
+                  const uint32_t *d_taus, uint32_t N_tau, float *d_Fmn, tcw_result *d_result,
+                  int flags);
+
+/* The same with host buffers: copies in, computes, copies out, synchronises. */
+int tcw_map_plain_host(tcw_handle *h, const float *atoms, uint32_t numAtoms, uint32_t TAtom,
+                       uint32_t t0_data, int window, const uint32_t *t0s, uint32_t N_t0,
+                       const uint32_t *taus, uint32_t N_tau, float *Fmn, tcw_result *result,
+                       int flags);
+
+/* Batched form (no per-template map): a plan fixes the templates' geometry
+ * and grids and the tile schedule; runs take atoms and give one result per
+ * template.  Replaces the per-template loop of a transient grid search
+ * (grid_based_searches.py:1186-1189) over call_compute_transient_fstat_map. */
+int tcw_plan_create(tcw_handle *h, const tcw_template_desc *desc, uint32_t n_templates,
+                    const uint32_t *t0s, uint64_t n_t0s, const uint32_t *taus, uint64_t n_taus,
+                    const tcw_tile_config *cfg, int flags, tcw_plan **plan);
+int tcw_plan_destroy(tcw_plan *plan);
+int tcw_plan_info(const tcw_plan *plan, uint64_t *n_cells, uint32_t *n_items,
+                  uint64_t *n_atom_rows, tcw_tile_config *cfg);
+/* use_graph != 0: the first run captures the launch sequence into a CUDA
+ * graph owned by the plan; later runs replay it (same d_atoms/d_results
+ * pointers required; different pointers re-capture). */
+int tcw_plan_run(tcw_handle *h, tcw_plan *plan, const float *d_atoms, tcw_result *d_results,
+                 int use_graph);
+int tcw_plan_run_host(tcw_handle *h, tcw_plan *plan, const float *atoms, tcw_result *results);
+/* One run without a graph, with CUDA events between its kernels on the
+ * handle's stream; synchronises and writes the durations (ms) of the prefix,
+ * map and finalize kernels to ms[0..2].  For measurement. */
+int tcw_plan_run_timed(tcw_handle *h, tcw_plan *plan, const float *d_atoms, tcw_result *d_results,
+                       float *ms);
+
+/* Measured throughput of `device` for roofline denominators: FP32 and FP64
+ * FMA in TFLOP/s (an FMA counts 2) and MUFU ex2 in Tops/s.  A measurement
+ * utility; it has no counterpart in the reference. */
+int tcw_probe_peaks(int device, double *fp32_tflops, double *fp64_tflops, double *mufu_tops);
+
+/* Test hook: make the n-th following workspace allocation on this handle
+ * fail (n = 0 disables).  Host-side only; used to test error paths. */
+int tcw_debug_fail_alloc(tcw_handle *h, int n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TCW_B200_H */

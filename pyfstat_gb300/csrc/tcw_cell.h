@@ -1,0 +1,544 @@
+// Per-cell arithmetic of the transient F-statistic map, shared by the CUDA
+// kernels and a host build used only by the test-suite to check the
+// algorithm against the oracle on the CPU.
+//
+// Reference semantics followed (PyFstat pyfstat/pyCUDAkernels/):
+//   * atom index of a window start, cudaTransientFstatRectWindow.cu:21-31
+//   * atom index of a window end,   cudaTransientFstatRectWindow.cu:54-69
+//   * exponential window weights and truncation at t0 + 3 tau,
+//     cudaTransientFstatExpWindow.cu:22, :53, :80-101
+//   * conditioning test and F,      cudaTransientFstatRectWindow.cu:93-118
+// all in u32 time arithmetic, wrap-around included.
+//
+// Precision design (the reference sums in FP32 and loses up to ~4e-4 of 2F
+// on short windows, where D = A B - C^2 cancels):
+//   * window sums are carried as unevaluated FP32 pairs (hi + lo);
+//   * D = A B - C^2 and G = B Fa - C Fb are formed with error-free FMA
+//     products from those pairs, so cancellation in them costs nothing;
+//   * F = (|G|^2 + D |Fb|^2) / (B D), which equals the reference's
+//     (B|Fa|^2 + A|Fb|^2 - 2C Re(Fa Fb*)) / D but is a sum of two non-negative
+//     terms (no cancellation);
+//   * the test cond < 1e4, cond = (A+B+disc)/(A+B-disc), is evaluated as
+//     (A+B+disc)^2 < 4e4 D, the same inequality without the cancelling
+//     denominator ((A+B+disc)(A+B-disc) = 4D).
+#pragma once
+
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define TCW_HD __host__ __device__ __forceinline__
+#else
+#define TCW_HD static inline
+#include <math.h>
+#endif
+
+namespace tcw {
+
+// ------------------------------------------------------------ rounding-exact ops
+// Error-free transformations need every operation rounded exactly once, in
+// the written order: on the device the _rn intrinsics are never contracted
+// into FMAs; the host build is compiled with -ffp-contract=off.
+TCW_HD float fadd(float a, float b) {
+#if defined(__CUDA_ARCH__)
+  return __fadd_rn(a, b);
+#else
+  return a + b;
+#endif
+}
+TCW_HD float fsub(float a, float b) {
+#if defined(__CUDA_ARCH__)
+  return __fsub_rn(a, b);
+#else
+  return a - b;
+#endif
+}
+TCW_HD float fmul(float a, float b) {
+#if defined(__CUDA_ARCH__)
+  return __fmul_rn(a, b);
+#else
+  return a * b;
+#endif
+}
+TCW_HD float ffma(float a, float b, float c) {
+#if defined(__CUDA_ARCH__)
+  return __fmaf_rn(a, b, c);
+#else
+  return fmaf(a, b, c);
+#endif
+}
+TCW_HD float fexp2(float x) {
+#if defined(__CUDA_ARCH__)
+  return exp2f(x);
+#else
+  return exp2f(x);
+#endif
+}
+
+// Unevaluated sum hi + lo.
+struct FF {
+  float h, l;
+};
+
+TCW_HD FF ff_zero() { return FF{0.0f, 0.0f}; }
+
+// Knuth TwoSum: s + e == a + b exactly.
+TCW_HD void two_sum(float a, float b, float &s, float &e) {
+  s = fadd(a, b);
+  float bb = fsub(s, a);
+  e = fadd(fsub(a, fsub(s, bb)), fsub(b, bb));
+}
+
+// x + r*E for a double-word E and a double-word constant r.
+TCW_HD FF ff_axpy(float x, FF r, FF E) {
+  float p = fmul(r.h, E.h);
+  float pe = ffma(r.h, E.h, -p);
+  pe = ffma(r.h, E.l, pe);
+  pe = ffma(r.l, E.h, pe);
+  float s, se;
+  two_sum(x, p, s, se);
+  return FF{s, fadd(se, pe)};
+}
+
+// Running sum: E + x.
+TCW_HD FF ff_add1(FF E, float x) {
+  float s, se;
+  two_sum(E.h, x, s, se);
+  return FF{s, fadd(E.l, se)};
+}
+
+// E1 - p*E2 (p a plain float, E2 a double-word).
+TCW_HD FF ff_sub_scaled(FF E1, float p, FF E2) {
+  float a = fmul(p, E2.h);
+  float ae = ffma(p, E2.h, -a);
+  ae = ffma(p, E2.l, ae);
+  float s, se;
+  two_sum(E1.h, -a, s, se);
+  return FF{s, fsub(fadd(se, E1.l), ae)};
+}
+
+// ------------------------------------------------------------ u32 division
+// Division of u32 by a per-template constant d >= 1 (Granlund & Montgomery,
+// "Division by invariant integers using multiplication", PLDI 1994, the
+// round-up variant with a 33-bit multiplier split as 2^32 + mul):
+//   l = ceil(log2 d), mul = floor(2^32 (2^l - d) / d) + 1,
+//   t = mulhi(x, mul), q = (t + ((x - t) >> 1)) >> (l - 1)  for d >= 2.
+struct FastDiv {
+  uint32_t d, mul, shift;  // shift = l; d == 1 handled separately
+};
+
+static inline FastDiv make_fastdiv(uint32_t d) {
+  FastDiv f;
+  f.d = d;
+  uint32_t l = 0;
+  while (l < 32 && ((uint64_t)1 << l) < d) l++;
+  f.shift = l;
+  if (d <= 1) {
+    f.mul = 0;
+  } else {
+    uint64_t num = (((uint64_t)1 << l) - d) << 32;
+    f.mul = (uint32_t)(num / d + 1);
+  }
+  return f;
+}
+
+TCW_HD uint32_t umulhi32(uint32_t a, uint32_t b) {
+#if defined(__CUDA_ARCH__)
+  return __umulhi(a, b);
+#else
+  return (uint32_t)(((uint64_t)a * (uint64_t)b) >> 32);
+#endif
+}
+
+TCW_HD uint32_t fdiv(uint32_t x, const FastDiv &f) {
+  if (f.d <= 1) return x;
+  uint32_t t = umulhi32(x, f.mul);
+  return (t + ((x - t) >> 1)) >> (f.shift - 1);
+}
+
+// ------------------------------------------------------------ template geometry
+struct Geom {
+  uint32_t numAtoms, TAtom, t0_data, half;
+  FastDiv div;
+};
+
+static inline Geom make_geom(uint32_t numAtoms, uint32_t TAtom, uint32_t t0_data) {
+  Geom g;
+  g.numAtoms = numAtoms;
+  g.TAtom = TAtom;
+  g.t0_data = t0_data;
+  g.half = TAtom / 2u;
+  g.div = make_fastdiv(TAtom);
+  return g;
+}
+
+// i_t0 (Rect.cu:21-31): u32 wrap, quotient assigned to int, clamped.
+TCW_HD uint32_t idx_start(uint32_t t0, const Geom &g) {
+  uint32_t q = fdiv(t0 - g.t0_data + g.half, g.div);
+  int32_t i = (int32_t)q;
+  if (i < 0) i = 0;
+  uint32_t u = (uint32_t)i;
+  return u < g.numAtoms ? u : g.numAtoms - 1u;
+}
+
+// i_t1 (Rect.cu:54-69): "- 1" applied to the unsigned quotient.
+TCW_HD uint32_t idx_end(uint32_t t1, const Geom &g) {
+  uint32_t q = fdiv(t1 - g.t0_data + g.half, g.div) - 1u;
+  int32_t i = (int32_t)q;
+  if (i < 0) i = 0;
+  uint32_t u = (uint32_t)i;
+  return u < g.numAtoms ? u : g.numAtoms - 1u;
+}
+
+// Atoms with non-zero exponential weight for a cell: indices in
+// [i_t0, i_t1] with t0 <= t_i <= t1 (Exp.cu:80-90), t_i = t0_data + i*TAtom,
+// t1 = t0 + 3 tau (u32).  Returns false for an empty window.
+TCW_HD bool exp_window(uint32_t t0, uint32_t tau, const Geom &g, uint32_t &lo,
+                       uint32_t &hi) {
+  uint32_t t1 = t0 + 3u * tau;
+  uint32_t a = idx_start(t0, g);
+  uint32_t b = idx_end(t1, g);
+  // first i with t_i >= t0
+  uint32_t first = 0;
+  if (t0 > g.t0_data) {
+    uint32_t d = t0 - g.t0_data;
+    uint32_t q = fdiv(d, g.div);
+    first = q + ((d - q * g.TAtom) != 0u ? 1u : 0u);
+  }
+  if (t1 < g.t0_data) return false;
+  uint32_t last = fdiv(t1 - g.t0_data, g.div);  // last i with t_i <= t1
+  lo = a > first ? a : first;
+  hi = b < last ? b : last;
+  return lo <= hi;
+}
+
+// ------------------------------------------------------------ F from window sums
+// Conditioning flag of a cell whose F fell back to 2 is reported by the
+// return value of fstat_ff through the `ok` out-parameter.
+template <bool kFp64Det>
+TCW_HD float fstat_ff(FF A, FF B, FF C, FF Far, FF Fai, FF Fbr, FF Fbi, bool &ok) {
+  // D = A B - C^2 with exact products of the high words
+  float p = fmul(A.h, B.h);
+  float pe = ffma(A.h, B.h, -p);
+  float q = fmul(C.h, C.h);
+  float qe = ffma(C.h, C.h, -q);
+  float corr = fsub(pe, qe);
+  corr = ffma(A.h, B.l, corr);
+  corr = ffma(A.l, B.h, corr);
+  corr = ffma(-2.0f * C.h, C.l, corr);
+  // low x low products matter: quantised prefix differences leave |lo| up to
+  // ~1e-4 |hi|, and cond/4 amplifies what is dropped from D
+  corr = ffma(A.l, B.l, corr);
+  corr = ffma(-C.l, C.l, corr);
+  float D;
+  if (kFp64Det) {
+    double Dd = (double)A.h * (double)B.h - (double)C.h * (double)C.h;
+    Dd += (double)(fadd(fadd(fmul(A.h, B.l), fmul(A.l, B.h)), fmul(-2.0f * C.h, C.l)));
+    Dd += (double)A.l * (double)B.l - (double)C.l * (double)C.l;
+    D = (float)Dd;
+  } else {
+    D = fadd(fsub(p, q), corr);
+  }
+  float sumAB = fadd(fadd(A.h, B.h), fadd(A.l, B.l));
+  float dAB = fadd(fsub(A.h, B.h), fsub(A.l, B.l));
+  float Cs = fadd(C.h, C.l);
+  float disc = sqrtf(ffma(dAB, dAB, fmul(4.0f * Cs, Cs)));
+  float t = fadd(sumAB, disc);
+  ok = (D > 0.0f) && (fmul(t, t) < fmul(4.0e4f, D));
+  if (!ok) return 2.0f;
+  // G = B Fa - C Fb, real and imaginary parts
+  float u, ue, v, ve;
+  u = fmul(B.h, Far.h);
+  ue = ffma(B.h, Far.h, -u);
+  v = fmul(C.h, Fbr.h);
+  ve = ffma(C.h, Fbr.h, -v);
+  float gc = fsub(ue, ve);
+  gc = ffma(B.h, Far.l, gc);
+  gc = ffma(B.l, Far.h, gc);
+  gc = ffma(-C.h, Fbr.l, gc);
+  gc = ffma(-C.l, Fbr.h, gc);
+  gc = ffma(B.l, Far.l, gc);
+  gc = ffma(-C.l, Fbr.l, gc);
+  float Gre = fadd(fsub(u, v), gc);
+  u = fmul(B.h, Fai.h);
+  ue = ffma(B.h, Fai.h, -u);
+  v = fmul(C.h, Fbi.h);
+  ve = ffma(C.h, Fbi.h, -v);
+  gc = fsub(ue, ve);
+  gc = ffma(B.h, Fai.l, gc);
+  gc = ffma(B.l, Fai.h, gc);
+  gc = ffma(-C.h, Fbi.l, gc);
+  gc = ffma(-C.l, Fbi.h, gc);
+  gc = ffma(B.l, Fai.l, gc);
+  gc = ffma(-C.l, Fbi.l, gc);
+  float Gim = fadd(fsub(u, v), gc);
+  float fbr = fadd(Fbr.h, Fbr.l), fbi = fadd(Fbi.h, Fbi.l);
+  float Fb2 = ffma(fbr, fbr, fmul(fbi, fbi));
+  float G2 = ffma(Gre, Gre, fmul(Gim, Gim));
+  float num = ffma(D, Fb2, G2);
+  float den = fmul(fadd(B.h, B.l), D);
+  return num / den;
+}
+
+// The uncompensated FP32 variant (plain sums, D = AB - C^2 in FP32, the
+// reference's numerator and conditioning formula in FP32) -- kept for the
+// precision report only.
+TCW_HD float fstat_plain32(float A, float B, float C, float Far, float Fai, float Fbr,
+                           float Fbi, bool &ok) {
+  float sumAB = fadd(A, B);
+  float diffAB = fsub(A, B);
+  float disc = sqrtf(fadd(fmul(diffAB, diffAB), fmul(fmul(4.0f, C), C)));
+  float denom = fsub(sumAB, disc);
+  float cond = denom > 0.0f ? fadd(sumAB, disc) / denom : INFINITY;
+  float D = fsub(fmul(A, B), fmul(C, C));
+  ok = (cond < 1.0e4f) && (D > 0.0f);
+  if (!ok) return 2.0f;
+  float num = fsub(fadd(fmul(B, fadd(fmul(Far, Far), fmul(Fai, Fai))),
+                        fmul(A, fadd(fmul(Fbr, Fbr), fmul(Fbi, Fbi)))),
+                   fmul(fmul(2.0f, C), fadd(fmul(Far, Fbr), fmul(Fai, Fbi))));
+  return num / D;
+}
+
+// ------------------------------------------------------------ prefix rows
+// Rectangular windows read exclusive prefix sums P(j) = sum_{i<j} x_i of the
+// seven channels, stored per atom index as 16 floats: hi[0..6], pad, lo[0..6],
+// pad.  The high words are integer multiples of a per-channel quantum
+// Q_c = 2^(e_c - 22) with sum_i |x_c(i)| < 2^e_c, so any difference of two of
+// them is exact in FP32; the low words carry the rest of the double-word
+// prefix.  A window sum is then (hi1 - hi0) + (lo1 - lo0) with one rounding
+// of size ~eps*Q in the low part.
+constexpr int kPrefixStride = 16;
+
+TCW_HD void rect_window_sums(const float *P0, const float *P1, FF W[7]) {
+#pragma unroll
+  for (int c = 0; c < 7; c++) {
+    W[c].h = fsub(P1[c], P0[c]);
+    W[c].l = fsub(P1[8 + c], P0[8 + c]);
+  }
+}
+
+// Quantum exponent for a channel with sum of |x| equal to sabs.
+TCW_HD float prefix_quantum(float sabs) {
+  // smallest power of two strictly above sabs (with margin), times 2^-22
+  float s = sabs * 1.01f + 1e-30f;
+  int e;
+  frexpf(s, &e);  // s = m * 2^e, 0.5 <= m < 1  ->  s < 2^e
+  return ldexpf(1.0f, e - 22);
+}
+
+// Quantise a double-word prefix value (h, l) into (hq, lo) with hq = k*Q.
+TCW_HD void quantise_prefix(float h, float l, float Q, float invQ, float &hq, float &lo) {
+  hq = fmul(rintf(fmul(h, invQ)), Q);
+  lo = fadd(fsub(h, hq), l);
+}
+
+
+// ------------------------------------------------------------ rectangular cell
+// End index of a rectangular window.  The reference extends a running sum
+// along tau (Rect.cu:75-91), so the summed range is [i_t0, max_{n'<=n} i_t1].
+// For a non-decreasing tau grid without u32 overflow of t0 + tau, i_t1 only
+// decreases where t1 + TAtom/2 < t0_data makes the u32 difference wrap (the
+// first taus of such a row); there i_t1 is the clamped last atom, so the
+// running maximum is max(i_t1(n), i_t1(tau_first)).
+TCW_HD uint32_t rect_end(uint32_t t0, uint32_t tau, uint32_t end_first, bool row_wrapped,
+                         const Geom &g) {
+  uint32_t e = idx_end(t0 + tau, g);
+  if (row_wrapped && end_first > e) e = end_first;
+  return e;
+}
+
+// Whether a row's first tau lies in the wrapped regime (t1 + TAtom/2 < t0_data).
+TCW_HD bool rect_row_wrapped(uint32_t t0, uint32_t tau_first, const Geom &g) {
+  return (uint64_t)t0 + (uint64_t)tau_first + (uint64_t)g.half < (uint64_t)g.t0_data;
+}
+
+template <bool kComp, bool kFp64Det>
+TCW_HD float rect_cell(const float *P, const float *P0, uint32_t j0, uint32_t e, bool &ok) {
+  if (e < j0) {  // empty window: zero sums, cond = inf
+    ok = false;
+    return 2.0f;
+  }
+  const float *P1 = P + (size_t)(e + 1u) * kPrefixStride;
+  FF W[7];
+  rect_window_sums(P0, P1, W);
+  if (kComp)
+    return fstat_ff<kFp64Det>(W[0], W[1], W[2], W[3], W[4], W[5], W[6], ok);
+  return fstat_plain32(W[0].h, W[1].h, W[2].h, W[3].h, W[4].h, W[5].h, W[6].h, ok);
+}
+
+// ------------------------------------------------------------ exponential column
+// One tau column over rows [m_begin, m_end), visited from the last row down.
+// With E(j) = sum_{J > i >= j} x_i r^(i-j) (r = e^(-TAtom/tau) for the F
+// channels, r^2 for A, B, C) the window sum of a cell is
+//     W = e^(-k (t_lo - t0)/tau) [E(lo) - r^(k L) E(hi+1)],  L = hi + 1 - lo.
+// The common factor e^(-k (t_lo - t0)/tau) scales A, B, C by s^2 and Fa, Fb by
+// s and cancels in F and in the conditioning test, so it is not applied.
+// Two backward recurrences (lower and upper window edge) walk down the atoms
+// as the rows descend; if a row's window lies above a pointer (only with u32
+// wrap-around in the grid) both restart from that row's window end.
+//
+// The subtraction is exact only if r^L matches the weights the recurrence
+// applied, so r^L is a double-word too: updated by one multiplication when L
+// moves by one, otherwise rebuilt by square-and-multiply.  A window whose
+// atoms are all zero (data gaps) has exactly zero sums and F = 2 in the
+// reference; it is detected exactly (first atom with a2 or b2 non-zero at or
+// above the lower pointer) instead of trusting a difference to cancel.
+struct ExpConsts {
+  FF r1, r2;   // e^(-TAtom/tau), e^(-2 TAtom/tau)
+  FF r1inv;    // e^(+TAtom/tau), valid when has_inv
+  bool has_inv;
+  float c1;    // TAtom / tau * log2(e) (uncompensated variant)
+};
+
+TCW_HD FF ff_from_double(double x) {
+  FF r;
+  r.h = (float)x;
+  r.l = (float)(x - (double)r.h);
+  return r;
+}
+
+TCW_HD ExpConsts exp_consts(uint32_t TAtom, uint32_t tau) {
+  ExpConsts k;
+  double x = (double)TAtom / (double)tau;
+  k.r1 = ff_from_double(exp(-x));
+  k.r2 = ff_from_double(exp(-2.0 * x));
+  k.has_inv = x < 60.0;
+  k.r1inv = k.has_inv ? ff_from_double(exp(x)) : FF{0.0f, 0.0f};
+  k.c1 = (float)(x * 1.4426950408889634);
+  return k;
+}
+
+// a*b for double-words, normalised.
+TCW_HD FF ff_mul(FF a, FF b) {
+  float p = fmul(a.h, b.h);
+  float e = ffma(a.h, b.h, -p);
+  e = ffma(a.h, b.l, e);
+  e = ffma(a.l, b.h, e);
+  float s = fadd(p, e);
+  return FF{s, fsub(e, fsub(s, p))};
+}
+
+TCW_HD FF ff_pow(FF r, uint32_t L) {
+  FF res{1.0f, 0.0f};
+  FF base = r;
+  while (L) {
+    if (L & 1u) res = ff_mul(res, base);
+    L >>= 1;
+    if (L) base = ff_mul(base, base);
+  }
+  return res;
+}
+
+// E1 - p*E2 with a double-word p.
+TCW_HD FF ff_sub_scaled2(FF E1, FF p, FF E2) {
+  float a = fmul(p.h, E2.h);
+  float ae = ffma(p.h, E2.h, -a);
+  ae = ffma(p.h, E2.l, ae);
+  ae = ffma(p.l, E2.h, ae);
+  float s, se;
+  two_sum(E1.h, -a, s, se);
+  return FF{s, fsub(fadd(se, E1.l), ae)};
+}
+
+template <bool kComp>
+TCW_HD void exp_step(FF E[7], const float *x, const ExpConsts &k) {
+  if (kComp) {
+#pragma unroll
+    for (int c = 0; c < 3; c++) E[c] = ff_axpy(x[c], k.r2, E[c]);
+#pragma unroll
+    for (int c = 3; c < 7; c++) E[c] = ff_axpy(x[c], k.r1, E[c]);
+  } else {
+#pragma unroll
+    for (int c = 0; c < 3; c++) E[c].h = ffma(k.r2.h, E[c].h, x[c]);
+#pragma unroll
+    for (int c = 3; c < 7; c++) E[c].h = ffma(k.r1.h, E[c].h, x[c]);
+  }
+}
+
+TCW_HD void load_atom(const float *__restrict__ p, float x[7]) {
+#pragma unroll
+  for (int c = 0; c < 7; c++) x[c] = p[c];
+}
+
+// Sink interface: sink(m, F, ok) for every row of the column.
+template <bool kComp, bool kFp64Det, class Sink>
+TCW_HD void exp_column(const float *__restrict__ atoms, const Geom &g,
+                       const uint32_t *__restrict__ t0s, uint32_t m_begin, uint32_t m_end,
+                       uint32_t tau, Sink &sink) {
+  const ExpConsts k = exp_consts(g.TAtom, tau);
+  FF Elo[7], Ehi[7];
+#pragma unroll
+  for (int c = 0; c < 7; c++) Elo[c] = Ehi[c] = ff_zero();
+  uint32_t J = 0, jL = 0, jH = 0;
+  uint32_t nz = 0xFFFFFFFFu;  // first atom >= jL with a2 or b2 non-zero
+  uint32_t Lp = 0;            // exponent of the cached power pw = r1^Lp
+  FF pw{1.0f, 0.0f};
+  bool init = false;
+  for (uint32_t mm = m_end; mm > m_begin; mm--) {
+    const uint32_t m = mm - 1u;
+    const uint32_t t0 = t0s[m];
+    uint32_t lo, hi;
+    if (!exp_window(t0, tau, g, lo, hi)) {
+      sink(m, 2.0f, false);
+      continue;
+    }
+    const uint32_t top = hi + 1u;
+    if (!init || top > J || lo > jL || top > jH) {
+      J = jL = jH = top;
+      nz = 0xFFFFFFFFu;
+#pragma unroll
+      for (int c = 0; c < 7; c++) Elo[c] = Ehi[c] = ff_zero();
+      init = true;
+    }
+    while (jH > top) {
+      jH--;
+      float x[7];
+      load_atom(atoms + (size_t)jH * 7u, x);
+      exp_step<kComp>(Ehi, x, k);
+    }
+    while (jL > lo) {
+      jL--;
+      float x[7];
+      load_atom(atoms + (size_t)jL * 7u, x);
+      exp_step<kComp>(Elo, x, k);
+      if (x[0] != 0.0f || x[1] != 0.0f) nz = jL;
+    }
+    if (nz > hi) {  // no data in the window: zero sums, cond = inf
+      sink(m, 2.0f, false);
+      continue;
+    }
+    FF W[7];
+    if (top == J) {
+#pragma unroll
+      for (int c = 0; c < 7; c++) W[c] = Elo[c];
+    } else if (kComp) {
+      const uint32_t L = top - lo;
+      if (L != Lp) {
+        if (L == Lp + 1u)
+          pw = ff_mul(pw, k.r1);
+        else if (L + 1u == Lp && k.has_inv)
+          pw = ff_mul(pw, k.r1inv);
+        else
+          pw = ff_pow(k.r1, L);
+        Lp = L;
+      }
+      const FF p2 = ff_mul(pw, pw);
+#pragma unroll
+      for (int c = 0; c < 3; c++) W[c] = ff_sub_scaled2(Elo[c], p2, Ehi[c]);
+#pragma unroll
+      for (int c = 3; c < 7; c++) W[c] = ff_sub_scaled2(Elo[c], pw, Ehi[c]);
+    } else {
+      const float p1 = fexp2(-(float)(top - lo) * k.c1);
+      const float p2 = fmul(p1, p1);
+#pragma unroll
+      for (int c = 0; c < 3; c++) W[c] = FF{ffma(-p2, Ehi[c].h, Elo[c].h), 0.0f};
+#pragma unroll
+      for (int c = 3; c < 7; c++) W[c] = FF{ffma(-p1, Ehi[c].h, Elo[c].h), 0.0f};
+    }
+    bool ok;
+    float F = kComp ? fstat_ff<kFp64Det>(W[0], W[1], W[2], W[3], W[4], W[5], W[6], ok)
+                    : fstat_plain32(W[0].h, W[1].h, W[2].h, W[3].h, W[4].h, W[5].h, W[6].h, ok);
+    sink(m, F, ok);
+  }
+}
+
+}  // namespace tcw

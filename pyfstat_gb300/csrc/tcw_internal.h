@@ -1,0 +1,72 @@
+// Internal device-side data structures shared by the kernels and the C-ABI
+// layer.  Not part of the public interface (include/tcw_b200.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "tcw_cell.h"
+
+namespace tcw {
+
+constexpr int kBlock = 128;  // threads per map block
+
+enum PrecisionMode : int {
+  kPrecFF = 0,        // double-word window sums, FP32 error-free D (default)
+  kPrecFF_F64Det = 1, // double-word window sums, native FP64 D
+  kPrecPlain32 = 2,   // uncompensated FP32 (precision report only)
+};
+
+// One template as the kernels see it.  Offsets index the concatenated
+// arrays of a call: atoms in rows of 7 floats, grids in u32 entries, prefix
+// rows of 16 floats, the output map in floats, per-item partials.
+struct TemplateDev {
+  uint64_t atom_off;
+  uint64_t t0_off;
+  uint64_t tau_off;
+  uint64_t p_off;
+  uint64_t map_off;
+  Geom g;
+  uint32_t window;  // 1 rect, 2 exp
+  uint32_t N_t0, N_tau;
+  uint32_t part_off, n_parts;
+  uint32_t pad;
+};
+
+// A tile of one template: rows [m0, m1) x columns [n0, n1).  For a
+// rectangular tile the block's threads are (tn columns) x (128/tn row lanes);
+// for an exponential tile each thread runs one column over a row chunk of
+// `rows_per_lane` rows.
+struct WorkItem {
+  uint32_t tmpl;
+  uint32_t part;
+  uint32_t m0, m1;
+  uint32_t n0, n1;
+  uint16_t tn;            // columns per block (32, 64 or 128)
+  uint16_t rows_per_lane; // exp only: rows per thread chunk
+  uint32_t pad;
+};
+
+// Per-item reduction result.  s = sum over the item's cells of exp(F - maxF).
+struct Partial {
+  float maxF;
+  uint32_t pad;
+  int64_t argmax;  // flat m*N_tau + n, smallest index among ties
+  double s;
+};
+
+// Launchers (tcw_kernels.cu).  All asynchronous on `stream`.
+cudaError_t launch_prefix(const TemplateDev *d_T, const uint32_t *d_rect_list, uint32_t n_rect,
+                          const float *d_atoms, float *d_P, int prec, cudaStream_t stream);
+cudaError_t launch_map(const TemplateDev *d_T, const WorkItem *d_items, uint32_t n_items,
+                       uint32_t *d_counter, uint32_t n_blocks, bool persistent, bool write_map,
+                       int prec, const float *d_atoms, const uint32_t *d_t0s,
+                       const uint32_t *d_taus, const float *d_P, float *d_Fmn, Partial *d_parts,
+                       cudaStream_t stream);
+cudaError_t launch_finalize(const TemplateDev *d_T, uint32_t n_templates, const Partial *d_parts,
+                            void *d_results, cudaStream_t stream);
+cudaError_t launch_posteriors(const TemplateDev *d_T, const float *d_Fmn, void *d_result,
+                              double *d_rowsum, double *d_colsum, uint32_t N_t0,
+                              uint32_t N_tau, cudaStream_t stream);
+
+}  // namespace tcw

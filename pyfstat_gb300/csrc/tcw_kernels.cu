@@ -1,0 +1,597 @@
+// CUDA kernels of the transient-CW F-statistic map for GB300 (sm_103a).
+//
+//   prefix_kernel    compensated exclusive prefix sums of the 7 atom channels of
+//                    each rectangular template (one block per template), stored
+//                    as quantised double-word rows (see tcw_cell.h)
+//   map_kernel       the (t0, tau) cells of a list of tiles; a block owns one tile
+//                    (grid launch) or pulls tiles from an atomic counter
+//                    (persistent launch).  Rectangular tiles difference two prefix
+//                    rows per cell; exponential tiles run two backward double-word
+//                    recurrences per tau column.  Every block reduces its cells to
+//                    (max F, first argmax, sum exp(F - max F)).
+//   finalize_kernel  per template, merges the tile partials in a fixed order:
+//                    maxF, argmax, lnBtSG in FP64.
+//   posterior kernels  row / column sums of exp(F - maxF) over a written map and
+//                    their argmax (t0 / tau max-posterior bins).
+// No tensor cores: nothing on this path is a dense contraction.
+#include <math.h>
+#include <stdint.h>
+
+#include "../../include/tcw_b200.h"
+#include "tcw_internal.h"
+
+namespace tcw {
+
+constexpr float kLog2e = 1.4426950408889634f;
+
+// ------------------------------------------------------------------ helpers
+
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  float s, e;
+  two_sum(a.h, b.h, s, e);
+  e = fadd(e, fadd(a.l, b.l));
+  float s2 = fadd(s, e);
+  return FF{s2, fsub(e, fsub(s2, s))};
+}
+
+__device__ __forceinline__ FF shfl_up_ff(FF v, int d) {
+  return FF{__shfl_up_sync(0xffffffffu, v.h, d), __shfl_up_sync(0xffffffffu, v.l, d)};
+}
+
+__device__ __forceinline__ void ld_row16(const float *p, float r[16]) {
+  const float4 *q = reinterpret_cast<const float4 *>(p);
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    float4 v = __ldg(q + k);
+    r[4 * k + 0] = v.x;
+    r[4 * k + 1] = v.y;
+    r[4 * k + 2] = v.z;
+    r[4 * k + 3] = v.w;
+  }
+}
+
+// ------------------------------------------------------------------ prefix
+
+template <bool kComp>
+__global__ void __launch_bounds__(256) prefix_kernel(const TemplateDev *__restrict__ T,
+                                                     const uint32_t *__restrict__ rect_list,
+                                                     const float *__restrict__ atoms,
+                                                     float *__restrict__ P) {
+  const TemplateDev t = T[rect_list[blockIdx.x]];
+  const uint32_t N = t.g.numAtoms;
+  const float *x = atoms + t.atom_off * 7u;
+  float *out = P + t.p_off * kPrefixStride;
+  const uint32_t tid = threadIdx.x, lane = tid & 31u, wid = tid >> 5;
+  const uint32_t chunk = (N + 255u) / 256u;
+  const uint32_t i0 = min(N, tid * chunk), i1 = min(N, i0 + chunk);
+
+  FF loc[7];
+  float sabs[7];
+#pragma unroll
+  for (int c = 0; c < 7; c++) {
+    loc[c] = ff_zero();
+    sabs[c] = 0.0f;
+  }
+  for (uint32_t i = i0; i < i1; i++) {
+#pragma unroll
+    for (int c = 0; c < 7; c++) {
+      float v = __ldg(x + (size_t)i * 7u + c);
+      loc[c] = kComp ? ff_add1(loc[c], v) : FF{fadd(loc[c].h, v), 0.0f};
+      sabs[c] += fabsf(v);
+    }
+  }
+
+  __shared__ FF warp_tot[8][7];
+  __shared__ float warp_abs[8][7];
+#pragma unroll
+  for (int c = 0; c < 7; c++) {
+    FF v = loc[c];
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      FF o = shfl_up_ff(v, d);
+      if (lane >= (uint32_t)d) v = kComp ? ff_add(o, v) : FF{fadd(o.h, v.h), 0.0f};
+    }
+    FF ex = shfl_up_ff(v, 1);
+    if (lane == 0) ex = ff_zero();
+    if (lane == 31) warp_tot[wid][c] = v;
+    loc[c] = ex;
+    float a = sabs[c];
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) a += __shfl_xor_sync(0xffffffffu, a, d);
+    if (lane == 0) warp_abs[wid][c] = a;
+  }
+  __syncthreads();
+
+  float Q[7], invQ[7];
+#pragma unroll
+  for (int c = 0; c < 7; c++) {
+    FF off = ff_zero();
+    for (uint32_t w = 0; w < wid; w++)
+      off = kComp ? ff_add(off, warp_tot[w][c]) : FF{fadd(off.h, warp_tot[w][c].h), 0.0f};
+    loc[c] = kComp ? ff_add(off, loc[c]) : FF{fadd(off.h, loc[c].h), 0.0f};
+    float S = 0.0f;
+    for (int w = 0; w < 8; w++) S += warp_abs[w][c];
+    Q[c] = prefix_quantum(S);
+    invQ[c] = 1.0f / Q[c];
+  }
+
+  auto write_row = [&](uint32_t j) {
+    float r[16];
+#pragma unroll
+    for (int c = 0; c < 7; c++) {
+      if (kComp) {
+        quantise_prefix(loc[c].h, loc[c].l, Q[c], invQ[c], r[c], r[8 + c]);
+      } else {
+        r[c] = loc[c].h;
+        r[8 + c] = 0.0f;
+      }
+    }
+    r[7] = 0.0f;
+    r[15] = 0.0f;
+    float4 *o = reinterpret_cast<float4 *>(out + (size_t)j * kPrefixStride);
+#pragma unroll
+    for (int k = 0; k < 4; k++) o[k] = make_float4(r[4 * k], r[4 * k + 1], r[4 * k + 2], r[4 * k + 3]);
+  };
+
+  for (uint32_t i = i0; i < i1; i++) {
+    write_row(i);
+#pragma unroll
+    for (int c = 0; c < 7; c++) {
+      float v = __ldg(x + (size_t)i * 7u + c);
+      loc[c] = kComp ? ff_add1(loc[c], v) : FF{fadd(loc[c].h, v), 0.0f};
+    }
+  }
+  if (i0 < N && i1 == N) write_row(N);
+}
+
+// ------------------------------------------------------------------ reductions
+
+struct Red {
+  float best;
+  int64_t bidx;
+  float mx, s, c;  // online sum of exp(F - mx), Kahan-compensated
+
+  __device__ __forceinline__ void init() {
+    best = -INFINITY;
+    bidx = INT64_MAX;
+    mx = -INFINITY;
+    s = 0.0f;
+    c = 0.0f;
+  }
+  __device__ __forceinline__ void add_term(float e) {
+    float y = fsub(e, c);
+    float t = fadd(s, y);
+    c = fsub(fsub(t, s), y);
+    s = t;
+  }
+  __device__ __forceinline__ void add(float F, int64_t idx) {
+    if (F != F) return;  // NaN cells are skipped
+    if (F > best || (F == best && idx < bidx)) {
+      best = F;
+      bidx = idx;
+    }
+    if (F > mx) {
+      float sc = exp2f((mx - F) * kLog2e);
+      s *= sc;
+      c *= sc;
+      mx = F;
+      add_term(1.0f);
+    } else {
+      add_term(exp2f((F - mx) * kLog2e));
+    }
+  }
+};
+
+struct RedVal {
+  float best;
+  int64_t bidx;
+  float mx, s;
+};
+
+__device__ __forceinline__ RedVal red_combine(RedVal a, RedVal b) {
+  RedVal r;
+  if (b.best > a.best || (b.best == a.best && b.bidx < a.bidx)) {
+    r.best = b.best;
+    r.bidx = b.bidx;
+  } else {
+    r.best = a.best;
+    r.bidx = a.bidx;
+  }
+  if (a.mx == -INFINITY) {
+    r.mx = b.mx;
+    r.s = b.s;
+  } else if (b.mx == -INFINITY) {
+    r.mx = a.mx;
+    r.s = a.s;
+  } else {
+    float M = fmaxf(a.mx, b.mx);
+    r.mx = M;
+    r.s = a.s * exp2f((a.mx - M) * kLog2e) + b.s * exp2f((b.mx - M) * kLog2e);
+  }
+  return r;
+}
+
+__device__ __forceinline__ RedVal shfl_down_red(RedVal v, int d) {
+  RedVal o;
+  o.best = __shfl_down_sync(0xffffffffu, v.best, d);
+  o.bidx = __shfl_down_sync(0xffffffffu, v.bidx, d);
+  o.mx = __shfl_down_sync(0xffffffffu, v.mx, d);
+  o.s = __shfl_down_sync(0xffffffffu, v.s, d);
+  return o;
+}
+
+// Reduce a block's per-thread reducers and write one Partial (thread 0).
+__device__ void block_reduce_store(const Red &red, Partial *out) {
+  __shared__ RedVal sh[kBlock / 32];
+  RedVal v{red.best, red.bidx, red.mx, fsub(red.s, red.c)};
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) v = red_combine(v, shfl_down_red(v, d));
+  const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    RedVal r = sh[0];
+    for (int w = 1; w < kBlock / 32; w++) r = red_combine(r, sh[w]);
+    Partial p;
+    p.maxF = r.best;
+    p.pad = 0;
+    p.argmax = r.bidx;
+    // s is relative to mx, which equals best for any non-empty item
+    p.s = (r.mx == -INFINITY) ? 0.0 : (double)r.s * (double)exp2f((r.mx - r.best) * kLog2e);
+    *out = p;
+  }
+  __syncthreads();
+}
+
+// ------------------------------------------------------------------ tiles
+
+template <int kPrec>
+__device__ __forceinline__ float rect_cell_dev(const float *P, const float *row0, uint32_t j0,
+                                               uint32_t e, bool &ok) {
+  if (e < j0) {
+    ok = false;
+    return 2.0f;
+  }
+  float r1[16];
+  ld_row16(P + (size_t)(e + 1u) * kPrefixStride, r1);
+  FF W[7];
+#pragma unroll
+  for (int c = 0; c < 7; c++) {
+    W[c].h = fsub(r1[c], row0[c]);
+    W[c].l = fsub(r1[8 + c], row0[8 + c]);
+  }
+  if (kPrec == kPrecPlain32)
+    return fstat_plain32(W[0].h, W[1].h, W[2].h, W[3].h, W[4].h, W[5].h, W[6].h, ok);
+  if (kPrec == kPrecFF_F64Det)
+    return fstat_ff<true>(W[0], W[1], W[2], W[3], W[4], W[5], W[6], ok);
+  return fstat_ff<false>(W[0], W[1], W[2], W[3], W[4], W[5], W[6], ok);
+}
+
+template <bool kWrite, int kPrec>
+__device__ void rect_tile(const TemplateDev &t, const WorkItem &w,
+                          const uint32_t *__restrict__ t0s_all,
+                          const uint32_t *__restrict__ taus_all, const float *__restrict__ P_all,
+                          float *__restrict__ Fmn, Red &red) {
+  const uint32_t tn = w.tn, lanes = kBlock / tn;
+  const uint32_t col = threadIdx.x % tn, rl = threadIdx.x / tn;
+  const uint32_t n = w.n0 + col;
+  if (n >= w.n1) return;
+  const uint32_t *t0s = t0s_all + t.t0_off;
+  const uint32_t *taus = taus_all + t.tau_off;
+  const float *P = P_all + t.p_off * kPrefixStride;
+  const uint32_t tau_first = __ldg(taus);
+  const uint32_t tau = __ldg(taus + n);
+  for (uint32_t m = w.m0 + rl; m < w.m1; m += lanes) {
+    const uint32_t t0 = __ldg(t0s + m);
+    const uint32_t j0 = idx_start(t0, t.g);
+    const bool wr = rect_row_wrapped(t0, tau_first, t.g);
+    const uint32_t ef = wr ? idx_end(t0 + tau_first, t.g) : 0u;
+    const uint32_t e = rect_end(t0, tau, ef, wr, t.g);
+    float row0[16];
+    ld_row16(P + (size_t)j0 * kPrefixStride, row0);
+    bool ok;
+    const float F = rect_cell_dev<kPrec>(P, row0, j0, e, ok);
+    const int64_t idx = (int64_t)m * t.N_tau + n;
+    if (kWrite) Fmn[t.map_off + idx] = F;
+    red.add(F, idx);
+  }
+}
+
+template <bool kWrite>
+struct MapSink {
+  float *Fmn;
+  uint32_t N_tau, n;
+  Red *red;
+  __device__ __forceinline__ void operator()(uint32_t m, float F, bool) {
+    const int64_t idx = (int64_t)m * N_tau + n;
+    if (kWrite) Fmn[idx] = F;
+    red->add(F, idx);
+  }
+};
+
+template <bool kWrite, int kPrec>
+__device__ void exp_tile(const TemplateDev &t, const WorkItem &w, const float *__restrict__ atoms,
+                         const uint32_t *__restrict__ t0s_all,
+                         const uint32_t *__restrict__ taus_all, float *__restrict__ Fmn,
+                         Red &red) {
+  const uint32_t tn = w.tn;
+  const uint32_t col = threadIdx.x % tn, rl = threadIdx.x / tn;
+  const uint32_t n = w.n0 + col;
+  if (n >= w.n1) return;
+  const uint32_t R = w.rows_per_lane;
+  const uint32_t mb = w.m0 + rl * R;
+  if (mb >= w.m1) return;
+  const uint32_t me = min(w.m1, mb + R);
+  const uint32_t *t0s = t0s_all + t.t0_off;
+  const uint32_t tau = __ldg(taus_all + t.tau_off + n);
+  MapSink<kWrite> sink{kWrite ? Fmn + t.map_off : nullptr, t.N_tau, n, &red};
+  const float *x = atoms + t.atom_off * 7u;
+  if (kPrec == kPrecPlain32)
+    exp_column<false, false>(x, t.g, t0s, mb, me, tau, sink);
+  else if (kPrec == kPrecFF_F64Det)
+    exp_column<true, true>(x, t.g, t0s, mb, me, tau, sink);
+  else
+    exp_column<true, false>(x, t.g, t0s, mb, me, tau, sink);
+}
+
+template <bool kPersist, bool kWrite, int kPrec>
+__global__ void __launch_bounds__(kBlock)
+    map_kernel(const TemplateDev *__restrict__ T, const WorkItem *__restrict__ items,
+               uint32_t n_items, uint32_t *__restrict__ counter, const float *__restrict__ atoms,
+               const uint32_t *__restrict__ t0s, const uint32_t *__restrict__ taus,
+               const float *__restrict__ P, float *__restrict__ Fmn,
+               Partial *__restrict__ parts) {
+  __shared__ uint32_t s_item;
+  uint32_t it = blockIdx.x;
+  for (;;) {
+    if (kPersist) {
+      if (threadIdx.x == 0) s_item = atomicAdd(counter, 1u);
+      __syncthreads();
+      it = s_item;
+      __syncthreads();
+    }
+    if (it >= n_items) break;
+    const WorkItem w = items[it];
+    const TemplateDev t = T[w.tmpl];
+    Red red;
+    red.init();
+    if (t.window == TCW_WINDOW_RECT)
+      rect_tile<kWrite, kPrec>(t, w, t0s, taus, P, Fmn, red);
+    else
+      exp_tile<kWrite, kPrec>(t, w, atoms, t0s, taus, Fmn, red);
+    block_reduce_store(red, parts + w.part);
+    if (!kPersist) break;
+  }
+}
+
+// ------------------------------------------------------------------ finalize
+
+// One warp per template: merge its partials in index order.
+__global__ void __launch_bounds__(128) finalize_kernel(const TemplateDev *__restrict__ T,
+                                                       uint32_t n_templates,
+                                                       const Partial *__restrict__ parts,
+                                                       tcw_result *__restrict__ results) {
+  const uint32_t tmpl = blockIdx.x * 4u + (threadIdx.x >> 5);
+  const uint32_t lane = threadIdx.x & 31u;
+  if (tmpl >= n_templates) return;
+  const TemplateDev t = T[tmpl];
+  float best = -INFINITY;
+  int64_t bidx = INT64_MAX;
+  for (uint32_t k = lane; k < t.n_parts; k += 32) {
+    const Partial p = parts[t.part_off + k];
+    if (p.maxF > best || (p.maxF == best && p.argmax < bidx)) {
+      best = p.maxF;
+      bidx = p.argmax;
+    }
+  }
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) {
+    float ob = __shfl_xor_sync(0xffffffffu, best, d);
+    int64_t oi = __shfl_xor_sync(0xffffffffu, bidx, d);
+    if (ob > best || (ob == best && oi < bidx)) {
+      best = ob;
+      bidx = oi;
+    }
+  }
+  double S = 0.0;
+  for (uint32_t k = lane; k < t.n_parts; k += 32) {
+    const Partial p = parts[t.part_off + k];
+    if (p.s > 0.0) S += p.s * (double)exp2f((p.maxF - best) * kLog2e);
+  }
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) S += __shfl_xor_sync(0xffffffffu, S, d);
+  if (lane == 0) {
+    tcw_result r;
+    r.maxF = best;
+    r.argmax = bidx;
+    r.lnBtSG = log(70.0 / ((double)t.N_t0 * (double)t.N_tau)) + (double)best + log(S);
+    r.t0_mp_idx = -1;
+    r.tau_mp_idx = -1;
+    r.status = 0;
+    results[tmpl] = r;
+  }
+}
+
+// ------------------------------------------------------------------ posteriors
+
+constexpr uint32_t kColChunk = 64;
+
+__global__ void __launch_bounds__(256) rowsum_kernel(const float *__restrict__ Fmn,
+                                                     const tcw_result *__restrict__ res,
+                                                     uint32_t N_tau, double *__restrict__ rowsum) {
+  const float maxF = res->maxF;
+  const float *row = Fmn + (size_t)blockIdx.x * N_tau;
+  float s = 0.0f, c = 0.0f;
+  for (uint32_t n = threadIdx.x; n < N_tau; n += blockDim.x) {
+    float y = fsub(exp2f((row[n] - maxF) * kLog2e), c);
+    float t = fadd(s, y);
+    c = fsub(fsub(t, s), y);
+    s = t;
+  }
+  double v = (double)s - (double)c;
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+  __shared__ double sh[8];
+  if ((threadIdx.x & 31u) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot = 0.0;
+    for (int w = 0; w < 8; w++) tot += sh[w];
+    rowsum[blockIdx.x] = tot;
+  }
+}
+
+__global__ void __launch_bounds__(128) colsum_kernel(const float *__restrict__ Fmn,
+                                                     const tcw_result *__restrict__ res,
+                                                     uint32_t N_t0, uint32_t N_tau,
+                                                     double *__restrict__ colpart) {
+  const uint32_t n = blockIdx.x * 128u + threadIdx.x;
+  if (n >= N_tau) return;
+  const float maxF = res->maxF;
+  const uint32_t m0 = blockIdx.y * kColChunk, m1 = min(N_t0, m0 + kColChunk);
+  float s = 0.0f, c = 0.0f;
+  for (uint32_t m = m0; m < m1; m++) {
+    float y = fsub(exp2f((Fmn[(size_t)m * N_tau + n] - maxF) * kLog2e), c);
+    float t = fadd(s, y);
+    c = fsub(fsub(t, s), y);
+    s = t;
+  }
+  colpart[(size_t)blockIdx.y * N_tau + n] = (double)s - (double)c;
+}
+
+// First-occurrence argmax of the row sums and of the chunked column sums.
+__global__ void __launch_bounds__(1024) posterior_argmax_kernel(const double *__restrict__ rowsum,
+                                                                const double *__restrict__ colpart,
+                                                                uint32_t N_t0, uint32_t N_tau,
+                                                                uint32_t n_chunks,
+                                                                tcw_result *__restrict__ res) {
+  __shared__ double sv[32];
+  __shared__ int64_t si[32];
+  for (int pass = 0; pass < 2; pass++) {
+    const uint32_t N = pass == 0 ? N_t0 : N_tau;
+    double best = -1.0;
+    int64_t bidx = INT64_MAX;
+    for (uint32_t k = threadIdx.x; k < N; k += blockDim.x) {
+      double v;
+      if (pass == 0) {
+        v = rowsum[k];
+      } else {
+        v = 0.0;
+        for (uint32_t ch = 0; ch < n_chunks; ch++) v += colpart[(size_t)ch * N_tau + k];
+      }
+      if (v > best) {  // k increases within a thread: keeps the first
+        best = v;
+        bidx = k;
+      }
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+      double ob = __shfl_xor_sync(0xffffffffu, best, d);
+      int64_t oi = __shfl_xor_sync(0xffffffffu, bidx, d);
+      if (ob > best || (ob == best && oi < bidx)) {
+        best = ob;
+        bidx = oi;
+      }
+    }
+    if ((threadIdx.x & 31u) == 0) {
+      sv[threadIdx.x >> 5] = best;
+      si[threadIdx.x >> 5] = bidx;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      best = sv[0];
+      bidx = si[0];
+      for (uint32_t w = 1; w < blockDim.x / 32u; w++) {
+        if (sv[w] > best || (sv[w] == best && si[w] < bidx)) {
+          best = sv[w];
+          bidx = si[w];
+        }
+      }
+      if (pass == 0)
+        res->t0_mp_idx = bidx;
+      else
+        res->tau_mp_idx = bidx;
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------ launchers
+
+cudaError_t launch_prefix(const TemplateDev *d_T, const uint32_t *d_rect_list, uint32_t n_rect,
+                          const float *d_atoms, float *d_P, int prec, cudaStream_t stream) {
+  if (n_rect == 0) return cudaSuccess;
+  if (prec == kPrecPlain32)
+    prefix_kernel<false><<<n_rect, 256, 0, stream>>>(d_T, d_rect_list, d_atoms, d_P);
+  else
+    prefix_kernel<true><<<n_rect, 256, 0, stream>>>(d_T, d_rect_list, d_atoms, d_P);
+  return cudaGetLastError();
+}
+
+template <bool kPersist, bool kWrite>
+static void launch_map_prec(int prec, uint32_t grid, cudaStream_t s, const TemplateDev *T,
+                            const WorkItem *items, uint32_t n_items, uint32_t *counter,
+                            const float *atoms, const uint32_t *t0s, const uint32_t *taus,
+                            const float *P, float *Fmn, Partial *parts) {
+  if (prec == kPrecPlain32)
+    map_kernel<kPersist, kWrite, kPrecPlain32>
+        <<<grid, kBlock, 0, s>>>(T, items, n_items, counter, atoms, t0s, taus, P, Fmn, parts);
+  else if (prec == kPrecFF_F64Det)
+    map_kernel<kPersist, kWrite, kPrecFF_F64Det>
+        <<<grid, kBlock, 0, s>>>(T, items, n_items, counter, atoms, t0s, taus, P, Fmn, parts);
+  else
+    map_kernel<kPersist, kWrite, kPrecFF>
+        <<<grid, kBlock, 0, s>>>(T, items, n_items, counter, atoms, t0s, taus, P, Fmn, parts);
+}
+
+cudaError_t launch_map(const TemplateDev *d_T, const WorkItem *d_items, uint32_t n_items,
+                       uint32_t *d_counter, uint32_t n_blocks, bool persistent, bool write_map,
+                       int prec, const float *d_atoms, const uint32_t *d_t0s,
+                       const uint32_t *d_taus, const float *d_P, float *d_Fmn, Partial *d_parts,
+                       cudaStream_t stream) {
+  if (n_items == 0) return cudaSuccess;
+  if (persistent) {
+    if (write_map)
+      launch_map_prec<true, true>(prec, n_blocks, stream, d_T, d_items, n_items, d_counter,
+                                  d_atoms, d_t0s, d_taus, d_P, d_Fmn, d_parts);
+    else
+      launch_map_prec<true, false>(prec, n_blocks, stream, d_T, d_items, n_items, d_counter,
+                                   d_atoms, d_t0s, d_taus, d_P, d_Fmn, d_parts);
+  } else {
+    if (write_map)
+      launch_map_prec<false, true>(prec, n_items, stream, d_T, d_items, n_items, d_counter,
+                                   d_atoms, d_t0s, d_taus, d_P, d_Fmn, d_parts);
+    else
+      launch_map_prec<false, false>(prec, n_items, stream, d_T, d_items, n_items, d_counter,
+                                    d_atoms, d_t0s, d_taus, d_P, d_Fmn, d_parts);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(const TemplateDev *d_T, uint32_t n_templates, const Partial *d_parts,
+                            void *d_results, cudaStream_t stream) {
+  if (n_templates == 0) return cudaSuccess;
+  finalize_kernel<<<(n_templates + 3u) / 4u, 128, 0, stream>>>(
+      d_T, n_templates, d_parts, reinterpret_cast<tcw_result *>(d_results));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_posteriors(const TemplateDev *d_T, const float *d_Fmn, void *d_result,
+                              double *d_rowsum, double *d_colsum, uint32_t N_t0,
+                              uint32_t N_tau, cudaStream_t stream) {
+  (void)d_T;
+  tcw_result *res = reinterpret_cast<tcw_result *>(d_result);
+  rowsum_kernel<<<N_t0, 256, 0, stream>>>(d_Fmn, res, N_tau, d_rowsum);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const uint32_t n_chunks = (N_t0 + kColChunk - 1u) / kColChunk;
+  dim3 grid((N_tau + 127u) / 128u, n_chunks);
+  colsum_kernel<<<grid, 128, 0, stream>>>(d_Fmn, res, N_t0, N_tau, d_colsum);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  posterior_argmax_kernel<<<1, 1024, 0, stream>>>(d_rowsum, d_colsum, N_t0, N_tau, n_chunks,
+                                                  res);
+  return cudaGetLastError();
+}
+
+}  // namespace tcw

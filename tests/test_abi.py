@@ -1,0 +1,83 @@
+"""The C-ABI library builds, loads and exports every function the header
+declares; calls that need no GPU behave (no compute without a GPU)."""
+
+import ctypes
+import os
+import re
+
+import pytest
+
+from conftest import REPO
+
+HEADER = os.path.join(REPO, "include", "tcw_b200.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(tcw_[a-z0-9_]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from pyfstat_gb300 import _lib, build
+
+    build.build()
+    return _lib.load()
+
+
+def test_header_declares_the_entry_points():
+    names = declared_functions()
+    for required in ("tcw_create", "tcw_destroy", "tcw_map_plain", "tcw_map_plain_host",
+                     "tcw_plan_create", "tcw_plan_run", "tcw_plan_run_host", "tcw_sync",
+                     "tcw_strerror"):
+        assert required in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    from pyfstat_gb300 import _lib
+
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+        assert name in _lib.SIGNATURES, f"{name} has no ctypes signature"
+
+
+def test_struct_layouts():
+    from pyfstat_gb300 import _lib
+
+    assert ctypes.sizeof(_lib.TcwResult) == 40
+    assert ctypes.sizeof(_lib.TcwTemplateDesc) == 48
+    assert ctypes.sizeof(_lib.TcwTileConfig) == 20
+
+
+def test_calls_without_a_gpu(lib):
+    from pyfstat_gb300 import _lib
+
+    assert lib.tcw_abi_version() == 1
+    for code in range(-7, 1):
+        assert lib.tcw_strerror(code)
+    assert b"unknown" in lib.tcw_strerror(-99)
+    assert lib.tcw_destroy(None) == _lib.TCW_ERR_INVALID_ARG
+    assert lib.tcw_sync(None, 0) == _lib.TCW_ERR_INVALID_ARG
+    if _lib.device_count() == 0:
+        h = ctypes.c_void_p()
+        assert lib.tcw_create(ctypes.byref(h), 0) == _lib.TCW_ERR_NO_DEVICE
+        assert not h.value
+        with pytest.raises(_lib.TcwError):
+            _lib.Handle(0)
+
+
+def test_no_fallback_without_gpu():
+    """The b200 feature is reported unavailable without a device; asking for
+    it raises instead of falling back to the CPU."""
+    from pyfstat_gb300 import _lib
+    from pyfstat_gb300 import tcw_fstat_map_funcs as tcw
+
+    if _lib.device_count() > 0:
+        pytest.skip("a GPU is present")
+    features = tcw._get_transient_fstat_map_features()
+    assert features["b200"] is False
+    with pytest.raises(RuntimeError, match="b200 use was requested"):
+        tcw.init_transient_fstat_map_features("b200")
+    with pytest.raises(Exception, match="not available"):
+        tcw.call_compute_transient_fstat_map("b200", features, None, None)

@@ -1,0 +1,131 @@
+"""Batched plans (persistent kernel, CUDA graph) against the FP64 oracle and
+against the plain per-template path."""
+
+import numpy as np
+import pytest
+
+from _helpers import REL_TOL, rel_err
+from pyfstat_gb300 import synth
+from pyfstat_gb300.batched import TransientMapBatch, template_grids
+
+pytestmark = pytest.mark.gpu
+
+
+def small_templates(n=24, seed=3):
+    """Mixed rect/exp templates with uneven atom counts, gaps and grids small
+    enough for the CPU oracle."""
+    return synth.batched_templates(n, seed=seed, nsft_range=(30, 260), gap_range=(0.0, 0.3),
+                                   grid_range=(1, 90))
+
+
+def oracle_reference(oracle, t):
+    t0s, taus = template_grids(t)
+    F64, cond = oracle.map_f64(t["atoms"], t["TAtom"], t["t0_data"], t["window"], t0s, taus,
+                               with_cond=True)
+    return F64, cond
+
+
+@pytest.fixture(scope="module")
+def batch():
+    b = TransientMapBatch(small_templates())
+    yield b
+    b.close()
+
+
+def test_batched_matches_fp64_oracle(batch, oracle):
+    res = batch.run()
+    templates = small_templates()
+    for k, t in enumerate(templates):
+        F64, cond = oracle_reference(oracle, t)
+        band = np.abs(cond / 1e4 - 1) < 1e-5
+        assert float(res["maxF"][k]) == pytest.approx(F64.max(), rel=REL_TOL), k
+        if not band.any():
+            assert int(res["argmax"][k]) == int(np.argmax(F64)), k
+            assert float(res["lnBtSG"][k]) == pytest.approx(oracle.lnBtSG(F64), rel=REL_TOL,
+                                                            abs=1e-6), k
+
+
+def test_batched_equals_plain_path(batch):
+    from pyfstat_gb300 import _lib
+
+    res = batch.run()
+    h = batch.handle
+    for k, t in enumerate(small_templates()):
+        t0s, taus = template_grids(t)
+        F, r = h.map_plain_host(t["atoms"], t["TAtom"], t["t0_data"], t["window"], t0s, taus,
+                                want_map=True, flags=_lib.TCW_FLAG_LNBTSG)
+        # same per-cell arithmetic: identical max and argmax
+        assert float(res["maxF"][k]) == float(r["maxF"]), k
+        assert int(res["argmax"][k]) == int(r["argmax"]), k
+        assert float(res["lnBtSG"][k]) == pytest.approx(float(r["lnBtSG"]), rel=1e-9), k
+
+
+@pytest.mark.parametrize("cfg", [
+    dict(rect_tn=32, rect_tm=4, exp_tn=32, exp_rows=3, blocks_per_sm=2),
+    dict(rect_tn=64, rect_tm=16, exp_tn=64, exp_rows=0, blocks_per_sm=4),
+    dict(rect_tn=128, rect_tm=64, exp_tn=128, exp_rows=17, blocks_per_sm=16),
+])
+def test_tile_shapes_do_not_change_results(batch, cfg):
+    ref = batch.run()
+    b2 = TransientMapBatch(small_templates(), tile_config=cfg, handle=batch.handle)
+    try:
+        res = b2.run()
+    finally:
+        b2.close()
+    assert np.array_equal(res["maxF"], ref["maxF"])
+    assert np.array_equal(res["argmax"], ref["argmax"])
+    np.testing.assert_allclose(res["lnBtSG"], ref["lnBtSG"], rtol=1e-9)
+
+
+def test_graph_replay_on_device_buffers(batch):
+    torch = pytest.importorskip("torch")
+    from pyfstat_gb300 import _lib
+
+    dev = torch.device("cuda:0")
+    d_atoms = torch.from_numpy(batch.atoms).to(dev)
+    d_res = torch.zeros(batch.n_templates * 5, dtype=torch.float64, device=dev)
+    batch.handle.set_stream(torch.cuda.current_stream().cuda_stream)
+    try:
+        outs = []
+        for _ in range(3):
+            batch.run_device(d_atoms, d_res, use_graph=True)
+            torch.cuda.synchronize()
+            outs.append(d_res.cpu().numpy().view(_lib.RESULT_DTYPE).copy())
+        # new atoms through the same captured graph (same buffer, new contents)
+        d_atoms.mul_(2.0)
+        batch.run_device(d_atoms, d_res, use_graph=True)
+        torch.cuda.synchronize()
+        scaled = d_res.cpu().numpy().view(_lib.RESULT_DTYPE).copy()
+    finally:
+        batch.handle.set_stream(None)
+    ref = batch.run()
+    for o in outs:
+        assert np.array_equal(o["maxF"], ref["maxF"])
+        assert np.array_equal(o["argmax"], ref["argmax"])
+    # F is invariant under a common scale of a2,b2,ab by s and Fa,Fb by s...
+    # with s = 2 on all channels F scales by 2 (F ~ |F|^2 / M): maxF doubles
+    np.testing.assert_allclose(scaled["maxF"][ref["maxF"] != 2], 2 * ref["maxF"][ref["maxF"] != 2],
+                               rtol=1e-5)
+
+
+def test_single_cell_and_single_atom_templates(oracle):
+    t0_data, A = synth.merged_atoms(5, 1, 1, inject=None)
+    t0_data2, A2 = synth.merged_atoms(6, 40, 1)
+    templates = [
+        dict(window=1, atoms=A, TAtom=1800, t0_data=t0_data, t0=t0_data, dt0=1800, N_t0=1,
+             tau=1800, dtau=1800, N_tau=1),
+        dict(window=2, atoms=A2, TAtom=1800, t0_data=t0_data2, t0=t0_data2, dt0=1800, N_t0=1,
+             tau=1800 * 40, dtau=1, N_tau=1),
+        dict(window=1, atoms=A2, TAtom=1800, t0_data=t0_data2, t0=t0_data2, dt0=1800, N_t0=1,
+             tau=1800 * 40, dtau=1, N_tau=1),
+    ]
+    b = TransientMapBatch(templates)
+    try:
+        res = b.run()
+    finally:
+        b.close()
+    assert res["maxF"][0] == 2.0  # one atom: ill-conditioned -> F = 2
+    for k in (1, 2):
+        t = templates[k]
+        F64, _ = oracle_reference(oracle, t)
+        assert float(res["maxF"][k]) == pytest.approx(F64[0, 0], rel=REL_TOL)

@@ -1,0 +1,131 @@
+"""The device cell arithmetic (pyfstat_gb300/csrc/tcw_cell.h), built for the
+host, against the FP64 oracle and the reference's golden maps -- no GPU.
+
+This checks the algorithm the kernels run (quantised compensated prefixes,
+two-pointer exponential recurrences, error-free determinant, u32 index
+semantics); the GPU tests check the kernels themselves.
+"""
+
+import ctypes
+
+import numpy as np
+import pytest
+
+from _helpers import REL_TOL, golden_case, golden_cases, hc_map, rel_err
+from pyfstat_gb300 import synth
+
+P = ctypes.c_void_p
+
+
+def test_fastdiv_matches_integer_division(hostcell):
+    rng = np.random.default_rng(0)
+    xs = np.concatenate([np.arange(0, 200000, dtype=np.uint64),
+                         rng.integers(0, 2 ** 32, 500000, dtype=np.uint64),
+                         2 ** 32 - 1 - np.arange(20000, dtype=np.uint64)]).astype(np.uint32)
+    for d in [1, 2, 3, 5, 7, 60, 900, 1799, 1800, 1801, 3600, 65535, 65536, 86400, 2 ** 31 - 1,
+              2 ** 31, 2 ** 31 + 1, 2 ** 32 - 1]:
+        q = np.empty_like(xs)
+        hostcell.hc_fastdiv(ctypes.c_uint32(d), xs.ctypes.data_as(P), ctypes.c_uint64(xs.size),
+                            q.ctypes.data_as(P))
+        assert np.array_equal(q, xs // np.uint32(d)), d
+
+
+def test_exp_window_bounds_match_reference_loop(hostcell, oracle):
+    """[lo, hi] = atoms with t0 <= t_i <= t0 + 3 tau inside [i_t0, i_t1] (Exp.cu:80-90)."""
+    rng = np.random.default_rng(1)
+    n, TAtom, t0_data = 50, 1800, 700000000
+    t0s = (t0_data + rng.integers(-20000, 100000, 4000)).astype(np.uint32)
+    taus = rng.integers(1, 40000, 4000).astype(np.uint32)
+    lohi = np.empty((4000, 2), np.int32)
+    hostcell.hc_exp_window(ctypes.c_uint32(n), ctypes.c_uint32(TAtom), ctypes.c_uint32(t0_data),
+                           t0s.ctypes.data_as(P), taus.ctypes.data_as(P), ctypes.c_uint64(4000),
+                           lohi.ctypes.data_as(P))
+    for k in range(4000):
+        t0, tau = int(t0s[k]), int(taus[k])
+        t1 = (t0 + 3 * tau) & 0xFFFFFFFF
+        a = oracle.idx_start(t0, t0_data, TAtom, n)
+        b = oracle.idx_end(t1, t0_data, TAtom, n)
+        idx = [i for i in range(a, b + 1) if t0 <= t0_data + i * TAtom <= t1]
+        if idx:
+            assert (lohi[k, 0], lohi[k, 1]) == (idx[0], idx[-1]), k
+        else:
+            assert lohi[k, 0] > lohi[k, 1], k
+
+
+@pytest.mark.parametrize("case", ["rect", "exp"])
+def test_workload_maps_within_tolerance_of_fp64(hostcell, oracle, case):
+    c = synth.plain_rect_case() if case == "rect" else synth.plain_exp_case()
+    F64, cond = oracle.map_f64(c["atoms"], c["TAtom"], c["t0_data"], c["window"], c["t0s"],
+                               c["taus"], with_cond=True)
+    F, _ = hc_map(hostcell, c)
+    rel, nband = rel_err(F, F64, cond)
+    assert rel.max() < REL_TOL
+    assert np.argmax(F) == np.argmax(F64)
+    assert nband <= 2
+
+
+def test_uncompensated_variant_is_worse(hostcell, oracle):
+    """The plain-FP32 variant (precision report) misses the bar on the exp workload."""
+    c = synth.plain_exp_case()
+    F64, cond = oracle.map_f64(c["atoms"], c["TAtom"], c["t0_data"], 2, c["t0s"], c["taus"],
+                               with_cond=True)
+    F, _ = hc_map(hostcell, c, comp=False)
+    rel, _ = rel_err(F, F64, cond)
+    assert rel.max() > REL_TOL
+
+
+@pytest.mark.parametrize("row_chunk", [0, 1, 5, 33])
+def test_exp_row_chunks_agree(hostcell, oracle, row_chunk):
+    t0_data, A = synth.merged_atoms(9, 200, 2, gap_frac=0.15)
+    c = dict(window=2, atoms=A, TAtom=1800, t0_data=t0_data,
+             t0s=(t0_data + np.arange(120) * 1500 - 700).astype(np.uint32),
+             taus=np.round(1800 * np.logspace(0, 2.4, 70)).astype(np.uint32))
+    F64, cond = oracle.map_f64(A, 1800, t0_data, 2, c["t0s"], c["taus"], with_cond=True)
+    F, _ = hc_map(hostcell, c, row_chunk=row_chunk)
+    rel, _ = rel_err(F, F64, cond)
+    assert rel.max() < REL_TOL
+
+
+def test_golden_edge_cases(hostcell, oracle, golden):
+    """Every golden case (tiny grids, clamps, u32 wrap, off-grid steps, gaps,
+    the window-'none' cell, the reference test geometry): within tolerance of
+    FP64, same F = 2 fallback cells as the reference away from the threshold."""
+    for name in golden_cases(golden):
+        c = golden_case(golden, name)
+        F64, cond = oracle.map_f64(c["atoms"], c["TAtom"], c["t0_data"], c["window"], c["t0s"],
+                                   c["taus"], with_cond=True)
+        F, _ = hc_map(hostcell, c)
+        rel, _ = rel_err(F, F64, cond)
+        assert rel.max() < REL_TOL, (name, rel.max())
+        Fref = c["F"] if "F" in c else None
+        if Fref is not None:
+            clear = (cond > 1.01e4) | ~np.isfinite(cond)
+            assert np.all(F[clear] == 2.0) and np.all(Fref[clear] == 2.0), name
+
+
+def test_random_gappy_grids(hostcell, oracle):
+    """Random grids (off the atom grid, starting before the data, dtau = 0
+    included) over atoms with long runs of zero (gap) bins."""
+    for seed in range(16):
+        rng = np.random.default_rng(seed)
+        t0_data, A = synth.merged_atoms(seed, int(rng.integers(20, 300)), int(rng.integers(1, 3)),
+                                        gap_frac=float(rng.uniform(0, 0.5)))
+        A = A.copy()
+        for _ in range(int(rng.integers(0, 4))):
+            s = int(rng.integers(0, A.shape[0]))
+            A[s:s + int(rng.integers(1, 40))] = 0
+        for window in (1, 2):
+            nt0, ntau = int(rng.integers(1, 60)), int(rng.integers(1, 60))
+            t0 = int(t0_data + rng.integers(-5000, 3000))
+            t0s = (t0 + np.arange(nt0) * int(rng.integers(1, 4000))).astype(np.uint32)
+            taus = (int(rng.integers(1, 5000)) + np.arange(ntau) * int(rng.integers(0, 8000))
+                    ).astype(np.uint32)
+            c = dict(window=window, atoms=A, TAtom=1800, t0_data=t0_data, t0s=t0s, taus=taus)
+            F64, cond = oracle.map_f64(A, 1800, t0_data, window, t0s, taus, with_cond=True)
+            F, _ = hc_map(hostcell, c, row_chunk=int(rng.integers(0, 10)))
+            rel, _ = rel_err(F, F64, cond)
+            assert rel.max() < REL_TOL, (seed, window, rel.max())
+            port = oracle.rect_map_f32 if window == 1 else oracle.exp_map_f32
+            Fr = port(A, 1800, t0_data, t0s, taus)
+            clear = (cond > 1.01e4) | ~np.isfinite(cond)
+            assert np.all(F[clear] == 2.0) and np.all(Fr[clear] == 2.0), (seed, window)
