@@ -231,7 +231,9 @@ def run_ours(args, ws, rank, local):
         tile = json.loads(args.tile)
     batch = TransientMapBatch(templates, device=dev.index, tile_config=tile)
     h = batch.handle
-    stream = torch.cuda.current_stream(dev)
+    # a side stream: graphs cannot be captured on the legacy default stream
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
     h.set_stream(stream.cuda_stream)
     n_cells = batch.n_cells
     n_t = batch.n_templates

@@ -138,7 +138,8 @@ int tcw_plan_info(const tcw_plan *plan, uint64_t *n_cells, uint32_t *n_items,
                   uint64_t *n_atom_rows, tcw_tile_config *cfg);
 /* use_graph != 0: the first run captures the launch sequence into a CUDA
  * graph owned by the plan; later runs replay it (same d_atoms/d_results
- * pointers required; different pointers re-capture). */
+ * pointers required; different pointers re-capture).  On the legacy default
+ * stream (set_stream(NULL stream)) runs are launched without a graph. */
 int tcw_plan_run(tcw_handle *h, tcw_plan *plan, const float *d_atoms, tcw_result *d_results,
                  int use_graph);
 int tcw_plan_run_host(tcw_handle *h, tcw_plan *plan, const float *atoms, tcw_result *results);

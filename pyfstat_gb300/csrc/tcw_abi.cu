@@ -776,7 +776,8 @@ int tcw_plan_run(tcw_handle *h, tcw_plan *p, const float *d_atoms, tcw_result *d
     return set_err(h, TCW_ERR_INVALID_ARG, "plan and handle are on different devices");
   int rc = set_device(h);
   if (rc) return rc;
-  if (!use_graph) return plan_enqueue(h, p, d_atoms, d_results);
+  // stream capture is not allowed on the legacy default stream: run directly
+  if (!use_graph || h->stream == nullptr) return plan_enqueue(h, p, d_atoms, d_results);
   if (!p->gexec || p->g_atoms != d_atoms || p->g_results != d_results ||
       p->g_stream != h->stream) {
     if (p->gexec) {

@@ -84,7 +84,11 @@ def test_graph_replay_on_device_buffers(batch):
     dev = torch.device("cuda:0")
     d_atoms = torch.from_numpy(batch.atoms).to(dev)
     d_res = torch.zeros(batch.n_templates * 5, dtype=torch.float64, device=dev)
-    batch.handle.set_stream(torch.cuda.current_stream().cuda_stream)
+    side = torch.cuda.Stream(device=dev)
+    side.wait_stream(torch.cuda.current_stream())
+    batch.handle.set_stream(side.cuda_stream)
+    ctx = torch.cuda.stream(side)
+    ctx.__enter__()
     try:
         outs = []
         for _ in range(3):
@@ -97,6 +101,7 @@ def test_graph_replay_on_device_buffers(batch):
         torch.cuda.synchronize()
         scaled = d_res.cpu().numpy().view(_lib.RESULT_DTYPE).copy()
     finally:
+        ctx.__exit__(None, None, None)
         batch.handle.set_stream(None)
     ref = batch.run()
     for o in outs:
