@@ -51,6 +51,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--plain-templates", type=int, default=256,
                    help="templates timed with the plain per-template kernel")
+    p.add_argument("--window", choices=["both", "rect", "exp"], default="both",
+                   help="restrict the workload to one window type (breakdown runs)")
     p.add_argument("--tile", type=str, default="",
                    help="tile config as JSON, 'auto' for the autotuner, empty for defaults")
     return p.parse_args()
@@ -224,6 +226,9 @@ def run_ours(args, ws, rank, local):
     torch.cuda.set_device(dev)
 
     templates = workload(args.templates, args.seed + 1000003 * rank)
+    if args.window != "both":
+        keep = 1 if args.window == "rect" else 2
+        templates = [t for t in templates if t["window"] == keep]
     tile = None
     if args.tile == "auto":
         tile = "auto"

@@ -54,10 +54,16 @@ def test_batched_equals_plain_path(batch):
         t0s, taus = template_grids(t)
         F, r = h.map_plain_host(t["atoms"], t["TAtom"], t["t0_data"], t["window"], t0s, taus,
                                 want_map=True, flags=_lib.TCW_FLAG_LNBTSG)
-        # same per-cell arithmetic: identical max and argmax
-        assert float(res["maxF"][k]) == float(r["maxF"]), k
-        assert int(res["argmax"][k]) == int(r["argmax"]), k
-        assert float(res["lnBtSG"][k]) == pytest.approx(float(r["lnBtSG"]), rel=1e-9), k
+        # rect cells read the same prefix rows: identical; exp recurrences start
+        # where each tile's rows start, so values agree to rounding only
+        if t["window"] == 1:
+            assert float(res["maxF"][k]) == float(r["maxF"]), k
+            assert int(res["argmax"][k]) == int(r["argmax"]), k
+        else:
+            assert float(res["maxF"][k]) == pytest.approx(float(r["maxF"]), rel=2e-6), k
+            assert float(F.reshape(-1)[int(res["argmax"][k])]) == pytest.approx(
+                float(r["maxF"]), rel=2e-6), k
+        assert float(res["lnBtSG"][k]) == pytest.approx(float(r["lnBtSG"]), rel=1e-6), k
 
 
 @pytest.mark.parametrize("cfg", [
@@ -72,9 +78,11 @@ def test_tile_shapes_do_not_change_results(batch, cfg):
         res = b2.run()
     finally:
         b2.close()
-    assert np.array_equal(res["maxF"], ref["maxF"])
-    assert np.array_equal(res["argmax"], ref["argmax"])
-    np.testing.assert_allclose(res["lnBtSG"], ref["lnBtSG"], rtol=1e-9)
+    rect = batch.desc["window"] == 1
+    assert np.array_equal(res["maxF"][rect], ref["maxF"][rect])
+    assert np.array_equal(res["argmax"][rect], ref["argmax"][rect])
+    np.testing.assert_allclose(res["maxF"], ref["maxF"], rtol=2e-6)
+    np.testing.assert_allclose(res["lnBtSG"], ref["lnBtSG"], rtol=1e-6)
 
 
 def test_graph_replay_on_device_buffers(batch):
