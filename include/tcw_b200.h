@@ -85,8 +85,8 @@ typedef struct {
 
 /* Tile shapes of a batched plan (0 = library default / autotuned). */
 typedef struct {
-  uint32_t rect_tn;       /* columns per rect block: 32, 64 or 128 */
-  uint32_t rect_tm;       /* rows per rect tile */
+  uint32_t rect_tn;       /* columns per rect tile (any >= 1) */
+  uint32_t rect_tm;       /* rows per rect tile: 32, 64 or 128 (one thread per row) */
   uint32_t exp_tn;        /* columns per exp block: 32, 64 or 128 */
   uint32_t exp_rows;      /* rows per exp thread chunk (0 = whole column) */
   uint32_t blocks_per_sm; /* persistent blocks per SM */

@@ -203,7 +203,7 @@ void tile_template(uint32_t tmpl, const TemplateDev &t, const tcw_tile_config &c
         w.m1 = std::min(N_t0, m0 + tm);
         w.n0 = n0;
         w.n1 = std::min(N_tau, n0 + tn);
-        w.tn = (uint16_t)tn;
+        w.tn = (uint16_t)(tm / 32u);  // row groups of 32 rows (one per warp)
         w.rows_per_lane = 0;
         items.push_back(w);
         if (cost) cost->push_back((double)(w.m1 - w.m0) * (w.n1 - w.n0));
@@ -240,13 +240,13 @@ void tile_template(uint32_t tmpl, const TemplateDev &t, const tcw_tile_config &c
 void default_plain_cfg(const TemplateDev &t, tcw_tile_config &cfg, int n_sms) {
   const uint64_t target_blocks = (uint64_t)n_sms * 4u;
   if (t.window == TCW_WINDOW_RECT) {
-    cfg.rect_tn = t.N_tau >= 256 ? 64 : 32;
-    const uint32_t lanes = kBlock / cfg.rect_tn;
-    const uint64_t col_tiles = (t.N_tau + cfg.rect_tn - 1) / cfg.rect_tn;
-    uint64_t tm = (uint64_t)t.N_t0 * col_tiles / std::max<uint64_t>(1, target_blocks);
-    tm = std::max<uint64_t>(lanes, std::min<uint64_t>(64, tm));
-    tm = (tm + lanes - 1) / lanes * lanes;
-    cfg.rect_tm = (uint32_t)tm;
+    // 32-row tiles; columns per tile so that the grid has ~4 blocks per SM,
+    // at least 4 columns per warp and at most 256
+    cfg.rect_tm = 32;
+    const uint64_t row_tiles = (t.N_t0 + 31u) / 32u;
+    uint64_t tn = (uint64_t)t.N_tau * row_tiles / std::max<uint64_t>(1, target_blocks);
+    tn = std::max<uint64_t>(16, std::min<uint64_t>(256, tn));
+    cfg.rect_tn = (uint32_t)tn;
   } else {
     cfg.exp_tn = 32;
     // rows per thread: enough chunks for parallelism, long enough to amortise
@@ -257,12 +257,10 @@ void default_plain_cfg(const TemplateDev &t, tcw_tile_config &cfg, int n_sms) {
 }
 
 void fill_cfg_defaults(tcw_tile_config &c) {
-  if (c.rect_tn != 32 && c.rect_tn != 64 && c.rect_tn != 128) c.rect_tn = 128;
-  if (c.rect_tm == 0) c.rect_tm = 32;
+  if (c.rect_tm != 32 && c.rect_tm != 64 && c.rect_tm != 128) c.rect_tm = 128;
+  if (c.rect_tn == 0) c.rect_tn = 128;
   if (c.exp_tn != 32 && c.exp_tn != 64 && c.exp_tn != 128) c.exp_tn = 128;
   if (c.blocks_per_sm == 0) c.blocks_per_sm = 8;
-  uint32_t lanes = kBlock / c.rect_tn;
-  c.rect_tm = (c.rect_tm + lanes - 1) / lanes * lanes;
 }
 
 TemplateDev make_tdev(uint32_t numAtoms, uint32_t TAtom, uint32_t t0_data, int window,

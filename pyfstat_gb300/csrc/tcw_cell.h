@@ -74,6 +74,42 @@ TCW_HD float fexp2(float x) {
 #endif
 }
 
+// sqrt to ~2 ulp (feeds only the conditioning test).
+TCW_HD float sqrt_approx(float x) {
+#if defined(__CUDA_ARCH__)
+  float r;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+#else
+  return sqrtf(x);
+#endif
+}
+
+// a / b to ~1 ulp: approximate reciprocal, then one residual correction of
+// the quotient (q + r (a - b q)).
+TCW_HD float div_approx(float a, float b) {
+#if defined(__CUDA_ARCH__)
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(b));
+  float q = __fmul_rn(a, r);
+  float e = __fmaf_rn(-b, q, a);
+  return __fmaf_rn(e, r, q);
+#else
+  return a / b;
+#endif
+}
+
+// 2^x, ~2 ulp, flushes to 0 below the normal range (lnBtSG partial sums).
+TCW_HD float ex2_approx(float x) {
+#if defined(__CUDA_ARCH__)
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+#else
+  return exp2f(x);
+#endif
+}
+
 // Unevaluated sum hi + lo.
 struct FF {
   float h, l;
@@ -191,23 +227,33 @@ TCW_HD uint32_t idx_end(uint32_t t1, const Geom &g) {
 
 // Atoms with non-zero exponential weight for a cell: indices in
 // [i_t0, i_t1] with t0 <= t_i <= t1 (Exp.cu:80-90), t_i = t0_data + i*TAtom,
-// t1 = t0 + 3 tau (u32).  Returns false for an empty window.
-TCW_HD bool exp_window(uint32_t t0, uint32_t tau, const Geom &g, uint32_t &lo,
-                       uint32_t &hi) {
-  uint32_t t1 = t0 + 3u * tau;
-  uint32_t a = idx_start(t0, g);
-  uint32_t b = idx_end(t1, g);
-  // first i with t_i >= t0
-  uint32_t first = 0;
+// t1 = t0 + 3 tau (u32).  The lower end depends on t0 only, the upper end on
+// t0 + 3 tau.
+TCW_HD uint32_t exp_lo(uint32_t t0, const Geom &g) {
+  const uint32_t a = idx_start(t0, g);
+  uint32_t first = 0;  // first i with t_i >= t0
   if (t0 > g.t0_data) {
-    uint32_t d = t0 - g.t0_data;
-    uint32_t q = fdiv(d, g.div);
+    const uint32_t d = t0 - g.t0_data;
+    const uint32_t q = fdiv(d, g.div);
     first = q + ((d - q * g.TAtom) != 0u ? 1u : 0u);
   }
+  return a > first ? a : first;
+}
+
+// Upper end; false if no atom has t_i <= t1.
+TCW_HD bool exp_hi(uint32_t t0, uint32_t tau, const Geom &g, uint32_t &hi) {
+  const uint32_t t1 = t0 + 3u * tau;
   if (t1 < g.t0_data) return false;
-  uint32_t last = fdiv(t1 - g.t0_data, g.div);  // last i with t_i <= t1
-  lo = a > first ? a : first;
+  const uint32_t b = idx_end(t1, g);
+  const uint32_t last = fdiv(t1 - g.t0_data, g.div);  // last i with t_i <= t1
   hi = b < last ? b : last;
+  return true;
+}
+
+TCW_HD bool exp_window(uint32_t t0, uint32_t tau, const Geom &g, uint32_t &lo,
+                       uint32_t &hi) {
+  lo = exp_lo(t0, g);
+  if (!exp_hi(t0, tau, g, hi)) return false;
   return lo <= hi;
 }
 
@@ -241,7 +287,7 @@ TCW_HD float fstat_ff(FF A, FF B, FF C, FF Far, FF Fai, FF Fbr, FF Fbi, bool &ok
   float sumAB = fadd(fadd(A.h, B.h), fadd(A.l, B.l));
   float dAB = fadd(fsub(A.h, B.h), fsub(A.l, B.l));
   float Cs = fadd(C.h, C.l);
-  float disc = sqrtf(ffma(dAB, dAB, fmul(4.0f * Cs, Cs)));
+  float disc = sqrt_approx(ffma(dAB, dAB, fmul(4.0f * Cs, Cs)));
   float t = fadd(sumAB, disc);
   ok = (D > 0.0f) && (fmul(t, t) < fmul(4.0e4f, D));
   if (!ok) return 2.0f;
@@ -276,7 +322,44 @@ TCW_HD float fstat_ff(FF A, FF B, FF C, FF Far, FF Fai, FF Fbr, FF Fbi, bool &ok
   float G2 = ffma(Gre, Gre, fmul(Gim, Gim));
   float num = ffma(D, Fb2, G2);
   float den = fmul(fadd(B.h, B.l), D);
-  return num / den;
+  return div_approx(num, den);
+}
+
+// Tier 1: cells with cond < kFastCond (the bulk) in FP32 from the rounded
+// window sums.  Error bound there: D = fma(A, B, -C^2) has relative error
+// <= eps (2 A B / D + 1/2) <= 17.5 eps at cond = 32 ((cond+1)^2 / (4 cond)
+// bounds A B / D), and F = |G|^2/(B D) + |Fb|^2/B with G = B Fa - C Fb adds
+// <= 2 eps (1 + sqrt(cond)/2): about 1.5e-6 in all.  Returns false (and no
+// F) when the cell needs tier 2 (fstat_ff on the double-word sums).
+constexpr float kFastCond = 32.0f;
+
+TCW_HD bool fstat_fast(const FF W[7], float &F) {
+  const float A = fadd(W[0].h, W[0].l);
+  const float B = fadd(W[1].h, W[1].l);
+  const float C = fadd(W[2].h, W[2].l);
+  const float D = ffma(A, B, -fmul(C, C));
+  const float dAB = fsub(A, B);
+  const float disc = sqrt_approx(ffma(dAB, dAB, fmul(4.0f * C, C)));
+  const float t = fadd(fadd(A, B), disc);
+  if (!(fmul(t, t) < fmul(4.0f * kFastCond, D))) return false;
+  const float Far = fadd(W[3].h, W[3].l), Fai = fadd(W[4].h, W[4].l);
+  const float Fbr = fadd(W[5].h, W[5].l), Fbi = fadd(W[6].h, W[6].l);
+  const float Gre = ffma(B, Far, -fmul(C, Fbr));
+  const float Gim = ffma(B, Fai, -fmul(C, Fbi));
+  const float num = ffma(D, ffma(Fbr, Fbr, fmul(Fbi, Fbi)), ffma(Gre, Gre, fmul(Gim, Gim)));
+  F = div_approx(num, fmul(B, D));
+  return true;
+}
+
+// Both tiers for double-word window sums that are exact enough for tier 2.
+template <bool kFp64Det>
+TCW_HD float fstat_tiered(const FF W[7], bool &ok) {
+  float F;
+  if (fstat_fast(W, F)) {
+    ok = true;
+    return F;
+  }
+  return fstat_ff<kFp64Det>(W[0], W[1], W[2], W[3], W[4], W[5], W[6], ok);
 }
 
 // The uncompensated FP32 variant (plain sums, D = AB - C^2 in FP32, the
@@ -360,8 +443,7 @@ TCW_HD float rect_cell(const float *P, const float *P0, uint32_t j0, uint32_t e,
   const float *P1 = P + (size_t)(e + 1u) * kPrefixStride;
   FF W[7];
   rect_window_sums(P0, P1, W);
-  if (kComp)
-    return fstat_ff<kFp64Det>(W[0], W[1], W[2], W[3], W[4], W[5], W[6], ok);
+  if (kComp) return fstat_tiered<kFp64Det>(W, ok);
   return fstat_plain32(W[0].h, W[1].h, W[2].h, W[3].h, W[4].h, W[5].h, W[6].h, ok);
 }
 
@@ -396,17 +478,6 @@ TCW_HD FF ff_from_double(double x) {
   return r;
 }
 
-TCW_HD ExpConsts exp_consts(uint32_t TAtom, uint32_t tau) {
-  ExpConsts k;
-  double x = (double)TAtom / (double)tau;
-  k.r1 = ff_from_double(exp(-x));
-  k.r2 = ff_from_double(exp(-2.0 * x));
-  k.has_inv = x < 60.0;
-  k.r1inv = k.has_inv ? ff_from_double(exp(x)) : FF{0.0f, 0.0f};
-  k.c1 = (float)(x * 1.4426950408889634);
-  return k;
-}
-
 // a*b for double-words, normalised.
 TCW_HD FF ff_mul(FF a, FF b) {
   float p = fmul(a.h, b.h);
@@ -415,6 +486,30 @@ TCW_HD FF ff_mul(FF a, FF b) {
   e = ffma(a.l, b.h, e);
   float s = fadd(p, e);
   return FF{s, fsub(e, fsub(s, p))};
+}
+
+// 1/a for a double-word a > 0: FP32 reciprocal refined by one Newton step
+// in double-word arithmetic (relative error ~eps^2).
+TCW_HD FF ff_recip(FF a) {
+  const float y = 1.0f / a.h;
+  // e = 1 - a*y exactly enough: a.h*y via its exact product, then a.l*y
+  const float p = fmul(a.h, y);
+  const float pe = ffma(a.h, y, -p);
+  const float e = fsub(fsub(1.0f, p), ffma(a.l, y, pe));
+  const float yl = fmul(y, e);
+  const float s = fadd(y, yl);
+  return FF{s, fsub(yl, fsub(s, y))};
+}
+
+TCW_HD ExpConsts exp_consts(uint32_t TAtom, uint32_t tau) {
+  ExpConsts k;
+  const double x = (double)TAtom / (double)tau;
+  k.r1 = ff_from_double(exp(-x));
+  k.r2 = ff_mul(k.r1, k.r1);
+  k.has_inv = x < 60.0;
+  k.r1inv = k.has_inv ? ff_recip(k.r1) : FF{0.0f, 0.0f};
+  k.c1 = (float)(x * 1.4426950408889634);
+  return k;
 }
 
 TCW_HD FF ff_pow(FF r, uint32_t L) {
@@ -459,11 +554,25 @@ TCW_HD void load_atom(const float *__restrict__ p, float x[7]) {
   for (int c = 0; c < 7; c++) x[c] = p[c];
 }
 
-// Sink interface: sink(m, F, ok) for every row of the column.
+// E1 - p*E2 formed so that only the high-word subtraction rounds: when it
+// cancels (operands within a factor 2) it is exact, otherwise its rounding
+// is relative to the result.  Accurate to ~eps/2 of the window sum however
+// much of E1 the tail p*E2 removes -- enough for tier 1; tier 2 re-forms
+// the sum with ff_sub_scaled2.
+TCW_HD FF ff_sub_scaled_fast(FF E1, FF p, FF E2) {
+  const float a = fmul(p.h, E2.h);
+  float ae = ffma(p.h, E2.h, -a);
+  ae = ffma(p.h, E2.l, ae);
+  ae = ffma(p.l, E2.h, ae);
+  return FF{fsub(E1.h, a), fsub(E1.l, ae)};
+}
+
+// Sink interface: sink(m, F, ok) for every row of the column.  `lo_tab`, if
+// not null, holds exp_lo(t0s[m]) at lo_tab[m - m_begin].
 template <bool kComp, bool kFp64Det, class Sink>
 TCW_HD void exp_column(const float *__restrict__ atoms, const Geom &g,
                        const uint32_t *__restrict__ t0s, uint32_t m_begin, uint32_t m_end,
-                       uint32_t tau, Sink &sink) {
+                       uint32_t tau, Sink &sink, const uint32_t *lo_tab = nullptr) {
   const ExpConsts k = exp_consts(g.TAtom, tau);
   FF Elo[7], Ehi[7];
 #pragma unroll
@@ -476,8 +585,9 @@ TCW_HD void exp_column(const float *__restrict__ atoms, const Geom &g,
   for (uint32_t mm = m_end; mm > m_begin; mm--) {
     const uint32_t m = mm - 1u;
     const uint32_t t0 = t0s[m];
-    uint32_t lo, hi;
-    if (!exp_window(t0, tau, g, lo, hi)) {
+    const uint32_t lo = lo_tab ? lo_tab[m - m_begin] : exp_lo(t0, g);
+    uint32_t hi;
+    if (!exp_hi(t0, tau, g, hi) || lo > hi) {
       sink(m, 2.0f, false);
       continue;
     }
@@ -506,11 +616,25 @@ TCW_HD void exp_column(const float *__restrict__ atoms, const Geom &g,
       sink(m, 2.0f, false);
       continue;
     }
-    FF W[7];
-    if (top == J) {
+    bool ok;
+    float F;
+    if (!kComp) {
+      FF W[7];
+      if (top == J) {
 #pragma unroll
-      for (int c = 0; c < 7; c++) W[c] = Elo[c];
-    } else if (kComp) {
+        for (int c = 0; c < 7; c++) W[c] = Elo[c];
+      } else {
+        const float p1 = fexp2(-(float)(top - lo) * k.c1);
+        const float p2 = fmul(p1, p1);
+#pragma unroll
+        for (int c = 0; c < 3; c++) W[c] = FF{ffma(-p2, Ehi[c].h, Elo[c].h), 0.0f};
+#pragma unroll
+        for (int c = 3; c < 7; c++) W[c] = FF{ffma(-p1, Ehi[c].h, Elo[c].h), 0.0f};
+      }
+      F = fstat_plain32(W[0].h, W[1].h, W[2].h, W[3].h, W[4].h, W[5].h, W[6].h, ok);
+    } else if (top == J) {
+      F = fstat_tiered<kFp64Det>(Elo, ok);
+    } else {
       const uint32_t L = top - lo;
       if (L != Lp) {
         if (L == Lp + 1u)
@@ -522,21 +646,21 @@ TCW_HD void exp_column(const float *__restrict__ atoms, const Geom &g,
         Lp = L;
       }
       const FF p2 = ff_mul(pw, pw);
+      FF W[7];
 #pragma unroll
-      for (int c = 0; c < 3; c++) W[c] = ff_sub_scaled2(Elo[c], p2, Ehi[c]);
+      for (int c = 0; c < 3; c++) W[c] = ff_sub_scaled_fast(Elo[c], p2, Ehi[c]);
 #pragma unroll
-      for (int c = 3; c < 7; c++) W[c] = ff_sub_scaled2(Elo[c], pw, Ehi[c]);
-    } else {
-      const float p1 = fexp2(-(float)(top - lo) * k.c1);
-      const float p2 = fmul(p1, p1);
+      for (int c = 3; c < 7; c++) W[c] = ff_sub_scaled_fast(Elo[c], pw, Ehi[c]);
+      if (fstat_fast(W, F)) {
+        ok = true;
+      } else {
 #pragma unroll
-      for (int c = 0; c < 3; c++) W[c] = FF{ffma(-p2, Ehi[c].h, Elo[c].h), 0.0f};
+        for (int c = 0; c < 3; c++) W[c] = ff_sub_scaled2(Elo[c], p2, Ehi[c]);
 #pragma unroll
-      for (int c = 3; c < 7; c++) W[c] = FF{ffma(-p1, Ehi[c].h, Elo[c].h), 0.0f};
+        for (int c = 3; c < 7; c++) W[c] = ff_sub_scaled2(Elo[c], pw, Ehi[c]);
+        F = fstat_ff<kFp64Det>(W[0], W[1], W[2], W[3], W[4], W[5], W[6], ok);
+      }
     }
-    bool ok;
-    float F = kComp ? fstat_ff<kFp64Det>(W[0], W[1], W[2], W[3], W[4], W[5], W[6], ok)
-                    : fstat_plain32(W[0].h, W[1].h, W[2].h, W[3].h, W[4].h, W[5].h, W[6].h, ok);
     sink(m, F, ok);
   }
 }

@@ -147,14 +147,13 @@ __global__ void __launch_bounds__(256) prefix_kernel(const TemplateDev *__restri
 // ------------------------------------------------------------------ reductions
 
 struct Red {
-  float best;
-  int64_t bidx;
-  float mx, s, c;  // online sum of exp(F - mx), Kahan-compensated
+  float mx;        // running max F (= best)
+  int64_t bidx;    // its first flat index
+  float s, c;      // sum of exp(F - mx), Kahan-compensated
 
   __device__ __forceinline__ void init() {
-    best = -INFINITY;
-    bidx = INT64_MAX;
     mx = -INFINITY;
+    bidx = INT64_MAX;
     s = 0.0f;
     c = 0.0f;
   }
@@ -166,56 +165,45 @@ struct Red {
   }
   __device__ __forceinline__ void add(float F, int64_t idx) {
     if (F != F) return;  // NaN cells are skipped
-    if (F > best || (F == best && idx < bidx)) {
-      best = F;
-      bidx = idx;
-    }
     if (F > mx) {
-      float sc = exp2f((mx - F) * kLog2e);
+      const float sc = ex2_approx((mx - F) * kLog2e);
       s *= sc;
       c *= sc;
       mx = F;
+      bidx = idx;
       add_term(1.0f);
     } else {
-      add_term(exp2f((F - mx) * kLog2e));
+      if (F == mx && idx < bidx) bidx = idx;
+      add_term(ex2_approx((F - mx) * kLog2e));
     }
   }
 };
 
 struct RedVal {
-  float best;
+  float mx;
   int64_t bidx;
-  float mx, s;
+  float s;
 };
 
 __device__ __forceinline__ RedVal red_combine(RedVal a, RedVal b) {
+  if (a.mx == -INFINITY) return b;
+  if (b.mx == -INFINITY) return a;
   RedVal r;
-  if (b.best > a.best || (b.best == a.best && b.bidx < a.bidx)) {
-    r.best = b.best;
+  if (b.mx > a.mx || (b.mx == a.mx && b.bidx < a.bidx)) {
+    r.mx = b.mx;
     r.bidx = b.bidx;
   } else {
-    r.best = a.best;
+    r.mx = a.mx;
     r.bidx = a.bidx;
   }
-  if (a.mx == -INFINITY) {
-    r.mx = b.mx;
-    r.s = b.s;
-  } else if (b.mx == -INFINITY) {
-    r.mx = a.mx;
-    r.s = a.s;
-  } else {
-    float M = fmaxf(a.mx, b.mx);
-    r.mx = M;
-    r.s = a.s * exp2f((a.mx - M) * kLog2e) + b.s * exp2f((b.mx - M) * kLog2e);
-  }
+  r.s = a.s * ex2_approx((a.mx - r.mx) * kLog2e) + b.s * ex2_approx((b.mx - r.mx) * kLog2e);
   return r;
 }
 
 __device__ __forceinline__ RedVal shfl_down_red(RedVal v, int d) {
   RedVal o;
-  o.best = __shfl_down_sync(0xffffffffu, v.best, d);
-  o.bidx = __shfl_down_sync(0xffffffffu, v.bidx, d);
   o.mx = __shfl_down_sync(0xffffffffu, v.mx, d);
+  o.bidx = __shfl_down_sync(0xffffffffu, v.bidx, d);
   o.s = __shfl_down_sync(0xffffffffu, v.s, d);
   return o;
 }
@@ -223,7 +211,7 @@ __device__ __forceinline__ RedVal shfl_down_red(RedVal v, int d) {
 // Reduce a block's per-thread reducers and write one Partial (thread 0).
 __device__ void block_reduce_store(const Red &red, Partial *out) {
   __shared__ RedVal sh[kBlock / 32];
-  RedVal v{red.best, red.bidx, red.mx, fsub(red.s, red.c)};
+  RedVal v{red.mx, red.bidx, fsub(red.s, red.c)};
 #pragma unroll
   for (int d = 16; d > 0; d >>= 1) v = red_combine(v, shfl_down_red(v, d));
   const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
@@ -233,11 +221,10 @@ __device__ void block_reduce_store(const Red &red, Partial *out) {
     RedVal r = sh[0];
     for (int w = 1; w < kBlock / 32; w++) r = red_combine(r, sh[w]);
     Partial p;
-    p.maxF = r.best;
+    p.maxF = r.mx;
     p.pad = 0;
     p.argmax = r.bidx;
-    // s is relative to mx, which equals best for any non-empty item
-    p.s = (r.mx == -INFINITY) ? 0.0 : (double)r.s * (double)exp2f((r.mx - r.best) * kLog2e);
+    p.s = (r.mx == -INFINITY) ? 0.0 : (double)r.s;
     *out = p;
   }
   __syncthreads();
@@ -262,38 +249,68 @@ __device__ __forceinline__ float rect_cell_dev(const float *P, const float *row0
   }
   if (kPrec == kPrecPlain32)
     return fstat_plain32(W[0].h, W[1].h, W[2].h, W[3].h, W[4].h, W[5].h, W[6].h, ok);
-  if (kPrec == kPrecFF_F64Det)
-    return fstat_ff<true>(W[0], W[1], W[2], W[3], W[4], W[5], W[6], ok);
-  return fstat_ff<false>(W[0], W[1], W[2], W[3], W[4], W[5], W[6], ok);
+  return fstat_tiered<kPrec == kPrecFF_F64Det>(W, ok);
 }
 
+// Rectangular tile: each thread owns one row (t0) and walks the tile's
+// columns, so the row's start index, its prefix row and the u32-wrap state
+// are set up once per row; per cell only the end index and one prefix row
+// are needed.  The block's 4 warps are (rg row groups of 32 rows) x (4/rg
+// column ranges).  With a map to write, each warp transposes 32 x 32 blocks
+// through shared memory so that global stores are row-contiguous.
 template <bool kWrite, int kPrec>
 __device__ void rect_tile(const TemplateDev &t, const WorkItem &w,
                           const uint32_t *__restrict__ t0s_all,
                           const uint32_t *__restrict__ taus_all, const float *__restrict__ P_all,
-                          float *__restrict__ Fmn, Red &red) {
-  const uint32_t tn = w.tn, lanes = kBlock / tn;
-  const uint32_t col = threadIdx.x % tn, rl = threadIdx.x / tn;
-  const uint32_t n = w.n0 + col;
-  if (n >= w.n1) return;
+                          float *__restrict__ Fmn, Red &red, float *smw) {
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  const uint32_t rg = w.tn;  // row groups: 1, 2 or 4
+  const uint32_t cgs = 4u / rg;
+  const uint32_t my_rg = warp % rg, my_cg = warp / rg;
+  const uint32_t mbase = w.m0 + 32u * my_rg;
+  const uint32_t m = mbase + lane;
+  const bool row_ok = m < w.m1;
+  const uint32_t ncols = w.n1 - w.n0;
+  const uint32_t per = (ncols + cgs - 1u) / cgs;
+  const uint32_t nb = min(w.n1, w.n0 + my_cg * per), ne = min(w.n1, nb + per);
   const uint32_t *t0s = t0s_all + t.t0_off;
   const uint32_t *taus = taus_all + t.tau_off;
   const float *P = P_all + t.p_off * kPrefixStride;
   const uint32_t tau_first = __ldg(taus);
-  const uint32_t tau = __ldg(taus + n);
-  for (uint32_t m = w.m0 + rl; m < w.m1; m += lanes) {
-    const uint32_t t0 = __ldg(t0s + m);
-    const uint32_t j0 = idx_start(t0, t.g);
-    const bool wr = rect_row_wrapped(t0, tau_first, t.g);
-    const uint32_t ef = wr ? idx_end(t0 + tau_first, t.g) : 0u;
-    const uint32_t e = rect_end(t0, tau, ef, wr, t.g);
-    float row0[16];
+  uint32_t t0 = 0, j0 = 0, ef = 0;
+  bool wr = false;
+  float row0[16];
+  if (row_ok) {
+    t0 = __ldg(t0s + m);
+    j0 = idx_start(t0, t.g);
+    wr = rect_row_wrapped(t0, tau_first, t.g);
+    ef = wr ? idx_end(t0 + tau_first, t.g) : 0u;
     ld_row16(P + (size_t)j0 * kPrefixStride, row0);
-    bool ok;
-    const float F = rect_cell_dev<kPrec>(P, row0, j0, e, ok);
-    const int64_t idx = (int64_t)m * t.N_tau + n;
-    if (kWrite) Fmn[t.map_off + idx] = F;
-    red.add(F, idx);
+  }
+  const int64_t rowidx = (int64_t)m * t.N_tau;
+  for (uint32_t cb = nb; cb < ne; cb += 32u) {
+    const uint32_t ce = min(ne, cb + 32u);
+    for (uint32_t n = cb; n < ce; n++) {
+      const uint32_t tau = __ldg(taus + n);
+      float F = 2.0f;
+      if (row_ok) {
+        uint32_t e = idx_end(t0 + tau, t.g);
+        if (wr && ef > e) e = ef;
+        bool ok;
+        F = rect_cell_dev<kPrec>(P, row0, j0, e, ok);
+        red.add(F, rowidx + n);
+      }
+      if (kWrite) smw[lane * 33u + (n - cb)] = F;
+    }
+    if (kWrite) {
+      __syncwarp();
+      const uint32_t col = cb + lane;
+      for (uint32_t r = 0; r < 32u; r++) {
+        const uint32_t mr = mbase + r;
+        if (mr < w.m1 && col < ce) Fmn[t.map_off + (size_t)mr * t.N_tau + col] = smw[r * 33u + lane];
+      }
+      __syncwarp();
+    }
   }
 }
 
@@ -309,29 +326,42 @@ struct MapSink {
   }
 };
 
+// Exponential tile: each thread runs one tau column over a chunk of rows.
+// The lower window end depends on t0 only and is tabulated once per tile in
+// shared memory (lo_tab, kExpLoTab entries; longer tiles compute it inline).
+constexpr uint32_t kExpLoTab = 2048;
+
 template <bool kWrite, int kPrec>
 __device__ void exp_tile(const TemplateDev &t, const WorkItem &w, const float *__restrict__ atoms,
                          const uint32_t *__restrict__ t0s_all,
                          const uint32_t *__restrict__ taus_all, float *__restrict__ Fmn,
-                         Red &red) {
+                         Red &red, uint32_t *lo_tab) {
+  const uint32_t *t0s = t0s_all + t.t0_off;
+  const uint32_t rows = w.m1 - w.m0;
+  const bool use_tab = rows <= kExpLoTab;
+  if (use_tab) {
+    for (uint32_t r = threadIdx.x; r < rows; r += blockDim.x)
+      lo_tab[r] = exp_lo(__ldg(t0s + w.m0 + r), t.g);
+  }
+  __syncthreads();
   const uint32_t tn = w.tn;
   const uint32_t col = threadIdx.x % tn, rl = threadIdx.x / tn;
   const uint32_t n = w.n0 + col;
-  if (n >= w.n1) return;
   const uint32_t R = w.rows_per_lane;
   const uint32_t mb = w.m0 + rl * R;
-  if (mb >= w.m1) return;
-  const uint32_t me = min(w.m1, mb + R);
-  const uint32_t *t0s = t0s_all + t.t0_off;
-  const uint32_t tau = __ldg(taus_all + t.tau_off + n);
-  MapSink<kWrite> sink{kWrite ? Fmn + t.map_off : nullptr, t.N_tau, n, &red};
-  const float *x = atoms + t.atom_off * 7u;
-  if (kPrec == kPrecPlain32)
-    exp_column<false, false>(x, t.g, t0s, mb, me, tau, sink);
-  else if (kPrec == kPrecFF_F64Det)
-    exp_column<true, true>(x, t.g, t0s, mb, me, tau, sink);
-  else
-    exp_column<true, false>(x, t.g, t0s, mb, me, tau, sink);
+  if (n < w.n1 && mb < w.m1) {
+    const uint32_t me = min(w.m1, mb + R);
+    const uint32_t tau = __ldg(taus_all + t.tau_off + n);
+    MapSink<kWrite> sink{kWrite ? Fmn + t.map_off : nullptr, t.N_tau, n, &red};
+    const float *x = atoms + t.atom_off * 7u;
+    const uint32_t *tab = use_tab ? lo_tab + (mb - w.m0) : nullptr;
+    if (kPrec == kPrecPlain32)
+      exp_column<false, false>(x, t.g, t0s, mb, me, tau, sink, tab);
+    else if (kPrec == kPrecFF_F64Det)
+      exp_column<true, true>(x, t.g, t0s, mb, me, tau, sink, tab);
+    else
+      exp_column<true, false>(x, t.g, t0s, mb, me, tau, sink, tab);
+  }
 }
 
 template <bool kPersist, bool kWrite, int kPrec>
@@ -342,6 +372,10 @@ __global__ void __launch_bounds__(kBlock)
                const float *__restrict__ P, float *__restrict__ Fmn,
                Partial *__restrict__ parts) {
   __shared__ uint32_t s_item;
+  __shared__ union {
+    float warp_tile[kBlock / 32][32 * 33];  // rect map-write transposes
+    uint32_t lo[kExpLoTab];                 // exp window starts
+  } sm;
   uint32_t it = blockIdx.x;
   for (;;) {
     if (kPersist) {
@@ -356,9 +390,9 @@ __global__ void __launch_bounds__(kBlock)
     Red red;
     red.init();
     if (t.window == TCW_WINDOW_RECT)
-      rect_tile<kWrite, kPrec>(t, w, t0s, taus, P, Fmn, red);
+      rect_tile<kWrite, kPrec>(t, w, t0s, taus, P, Fmn, red, sm.warp_tile[threadIdx.x >> 5]);
     else
-      exp_tile<kWrite, kPrec>(t, w, atoms, t0s, taus, Fmn, red);
+      exp_tile<kWrite, kPrec>(t, w, atoms, t0s, taus, Fmn, red, sm.lo);
     block_reduce_store(red, parts + w.part);
     if (!kPersist) break;
   }

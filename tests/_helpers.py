@@ -66,3 +66,20 @@ def hc_map(lib, c, comp=True, row_chunk=0):
         lib.hc_exp_map(*args, ctypes.c_uint32(row_chunk), F.ctypes.data_as(P),
                        ok.ctypes.data_as(P))
     return F, ok.astype(bool)
+
+
+def argmax_ok(idx, F64, tol=REL_TOL):
+    """The flat argmax ``idx`` is the oracle's when the oracle's maximum is
+    unique within the tolerance; where several cells tie within it (windows
+    holding the same atoms, e.g. one merged bin between gaps) any of them."""
+    F64 = np.asarray(F64, dtype=np.float64).reshape(-1)
+    top = F64.max()
+    tied = np.flatnonzero(F64 >= top - 2 * tol * abs(top))
+    if tied.size == 1:
+        return int(idx) == int(tied[0])
+    return int(idx) in set(int(i) for i in tied)
+
+
+def index_ok(idx, values, tol=REL_TOL):
+    """Same rule for the argmax of a 1-D marginal (posterior row/column sums)."""
+    return argmax_ok(idx, values, tol)

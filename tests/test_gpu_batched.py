@@ -4,7 +4,7 @@ against the plain per-template path."""
 import numpy as np
 import pytest
 
-from _helpers import REL_TOL, rel_err
+from _helpers import REL_TOL, argmax_ok
 from pyfstat_gb300 import synth
 from pyfstat_gb300.batched import TransientMapBatch, template_grids
 
@@ -40,7 +40,7 @@ def test_batched_matches_fp64_oracle(batch, oracle):
         band = np.abs(cond / 1e4 - 1) < 1e-5
         assert float(res["maxF"][k]) == pytest.approx(F64.max(), rel=REL_TOL), k
         if not band.any():
-            assert int(res["argmax"][k]) == int(np.argmax(F64)), k
+            assert argmax_ok(res["argmax"][k], F64), k
             assert float(res["lnBtSG"][k]) == pytest.approx(oracle.lnBtSG(F64), rel=REL_TOL,
                                                             abs=1e-6), k
 
@@ -67,9 +67,9 @@ def test_batched_equals_plain_path(batch):
 
 
 @pytest.mark.parametrize("cfg", [
-    dict(rect_tn=32, rect_tm=4, exp_tn=32, exp_rows=3, blocks_per_sm=2),
-    dict(rect_tn=64, rect_tm=16, exp_tn=64, exp_rows=0, blocks_per_sm=4),
-    dict(rect_tn=128, rect_tm=64, exp_tn=128, exp_rows=17, blocks_per_sm=16),
+    dict(rect_tn=7, rect_tm=32, exp_tn=32, exp_rows=3, blocks_per_sm=2),
+    dict(rect_tn=64, rect_tm=64, exp_tn=64, exp_rows=0, blocks_per_sm=4),
+    dict(rect_tn=300, rect_tm=128, exp_tn=128, exp_rows=17, blocks_per_sm=16),
 ])
 def test_tile_shapes_do_not_change_results(batch, cfg):
     ref = batch.run()

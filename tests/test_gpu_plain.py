@@ -8,7 +8,7 @@ oracle's; lnBtSG within 1e-5 relative.
 import numpy as np
 import pytest
 
-from _helpers import REL_TOL, golden_case, golden_cases, rel_err
+from _helpers import REL_TOL, argmax_ok, golden_case, golden_cases, index_ok, rel_err
 from pyfstat_gb300 import synth
 
 pytestmark = pytest.mark.gpu
@@ -42,12 +42,13 @@ def _check_case(handle, oracle, c, flags=FLAGS_ALL, tol=REL_TOL):
     assert float(res["maxF"]) == float(F.max())
     assert int(res["argmax"]) == int(np.argmax(F))
     if nband == 0:
-        assert int(res["argmax"]) == int(np.argmax(F64)), c.get("name")
+        assert argmax_ok(res["argmax"], F64), c.get("name")
         lnB64 = oracle.lnBtSG(F64)
         assert float(res["lnBtSG"]) == pytest.approx(lnB64, rel=tol, abs=1e-6)
         if flags & 0x2:
-            assert int(res["t0_mp_idx"]) == oracle.t0_max_posterior_idx(F64)
-            assert int(res["tau_mp_idx"]) == oracle.tau_max_posterior_idx(F64)
+            e = np.exp(F64 - F64.max())
+            assert index_ok(res["t0_mp_idx"], e.sum(axis=1)), c.get("name")
+            assert index_ok(res["tau_mp_idx"], e.sum(axis=0)), c.get("name")
     return F, res
 
 
@@ -131,7 +132,7 @@ def test_device_pointer_entry_on_torch_stream(lib, handle, oracle):
                                with_cond=True)
     rel, _ = rel_err(F, F64, cond)
     assert rel.max() < REL_TOL
-    assert int(rec["argmax"]) == int(np.argmax(F64))
+    assert argmax_ok(rec["argmax"], F64)
 
 
 def test_errors_are_status_codes_and_handle_survives(lib, handle):
