@@ -89,7 +89,7 @@ typedef struct {
   uint32_t rect_tm;       /* rows per rect tile: 32, 64 or 128 (one thread per row) */
   uint32_t exp_tn;        /* columns per exp block: 32, 64 or 128 */
   uint32_t exp_rows;      /* rows per exp thread chunk (0 = whole column) */
-  uint32_t blocks_per_sm; /* persistent blocks per SM */
+  uint32_t blocks_per_sm; /* cap on persistent blocks per SM (occupancy limits it too) */
 } tcw_tile_config;
 
 typedef struct tcw_handle tcw_handle;
@@ -143,9 +143,10 @@ int tcw_plan_info(const tcw_plan *plan, uint64_t *n_cells, uint32_t *n_items,
 int tcw_plan_run(tcw_handle *h, tcw_plan *plan, const float *d_atoms, tcw_result *d_results,
                  int use_graph);
 int tcw_plan_run_host(tcw_handle *h, tcw_plan *plan, const float *atoms, tcw_result *results);
-/* One run without a graph, with CUDA events between its kernels on the
- * handle's stream; synchronises and writes the durations (ms) of the prefix,
- * map and finalize kernels to ms[0..2].  For measurement. */
+/* One run without a graph and with the two map kernels one after the other,
+ * CUDA events between the kernels on the handle's stream; synchronises and
+ * writes the durations (ms) of the prefix, rectangular-map, exponential-map
+ * and finalize kernels to ms[0..3].  For measurement. */
 int tcw_plan_run_timed(tcw_handle *h, tcw_plan *plan, const float *d_atoms, tcw_result *d_results,
                        float *ms);
 

@@ -293,8 +293,8 @@ class Plan:
                                   int(bool(use_graph))), self.handle.ptr)
 
     def run_timed(self, d_atoms, d_results):
-        """One run with per-kernel CUDA events: (prefix, map, finalize) ms."""
-        ms = (ctypes.c_float * 3)()
+        """One run with per-kernel CUDA events: (prefix, rect map, exp map, finalize) ms."""
+        ms = (ctypes.c_float * 4)()
         check(load().tcw_plan_run_timed(self.handle.ptr, self._p, _p(d_atoms), _p(d_results), ms),
               self.handle.ptr)
         return tuple(float(x) for x in ms)

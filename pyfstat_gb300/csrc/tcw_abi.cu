@@ -25,6 +25,9 @@ struct tcw_handle {
   int n_sms = 0;
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
+  cudaStream_t side_stream = nullptr;  // second branch of batched runs
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+  int prio_high = 0, prio_low = 0;
   char *d_ws = nullptr;
   size_t ws_cap = 0;
   char *h_stage = nullptr;
@@ -39,14 +42,16 @@ struct tcw_handle {
 struct tcw_plan {
   int device = 0;
   int prec = kPrecFF;
-  uint32_t n_templates = 0, n_items = 0, n_rect = 0, n_blocks = 0;
+  uint32_t n_templates = 0, n_items = 0, n_rect = 0;
+  uint32_t n_items_rect = 0, n_items_exp = 0, n_blocks_rect = 0, n_blocks_exp = 0;
   uint64_t n_cells = 0, n_atom_rows = 0, p_rows = 0;
   tcw_tile_config cfg{};
   char *d_buf = nullptr;  // one allocation for all plan-owned device arrays
   TemplateDev *d_T = nullptr;
   WorkItem *d_items = nullptr;
   Partial *d_parts = nullptr;
-  uint32_t *d_rect_list = nullptr, *d_t0s = nullptr, *d_taus = nullptr, *d_counter = nullptr;
+  uint32_t *d_rect_list = nullptr, *d_t0s = nullptr, *d_taus = nullptr;
+  uint32_t *d_counter = nullptr;  // [0] rect tiles, [1] exp tiles
   float *d_P = nullptr;
   // graph state
   cudaGraphExec_t gexec = nullptr;
@@ -260,7 +265,7 @@ void fill_cfg_defaults(tcw_tile_config &c) {
   if (c.rect_tm != 32 && c.rect_tm != 64 && c.rect_tm != 128) c.rect_tm = 128;
   if (c.rect_tn == 0) c.rect_tn = 128;
   if (c.exp_tn != 32 && c.exp_tn != 64 && c.exp_tn != 128) c.exp_tn = 128;
-  if (c.blocks_per_sm == 0) c.blocks_per_sm = 8;
+  if (c.blocks_per_sm == 0) c.blocks_per_sm = 32;  // cap; occupancy decides below it
 }
 
 TemplateDev make_tdev(uint32_t numAtoms, uint32_t TAtom, uint32_t t0_data, int window,
@@ -362,6 +367,15 @@ int tcw_create(tcw_handle **out, int device) {
     return TCW_ERR_CUDA;
   }
   h->stream = h->own_stream;
+  if (cudaDeviceGetStreamPriorityRange(&h->prio_low, &h->prio_high) != cudaSuccess ||
+      cudaStreamCreateWithPriority(&h->side_stream, cudaStreamNonBlocking, h->prio_low) !=
+          cudaSuccess ||
+      cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->join_ev, cudaEventDisableTiming) != cudaSuccess) {
+    cudaGetLastError();
+    tcw_destroy(h);
+    return TCW_ERR_CUDA;
+  }
   *out = h;
   return TCW_OK;
 }
@@ -373,6 +387,12 @@ int tcw_destroy(tcw_handle *h) {
   if (h->d_ws) cudaFree(h->d_ws);
   if (h->h_stage) cudaFreeHost(h->h_stage);
   if (h->stage_ev) cudaEventDestroy(h->stage_ev);
+  if (h->side_stream) {
+    cudaStreamSynchronize(h->side_stream);
+    cudaStreamDestroy(h->side_stream);
+  }
+  if (h->fork_ev) cudaEventDestroy(h->fork_ev);
+  if (h->join_ev) cudaEventDestroy(h->join_ev);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   cudaGetLastError();
   delete h;
@@ -477,9 +497,21 @@ static int plain_enqueue(tcw_handle *h, const float *d_atoms, uint32_t numAtoms,
   if (window == TCW_WINDOW_RECT)
     TCW_CUDA(h, launch_prefix(dT, reinterpret_cast<const uint32_t *>(ws + o_list), 1, d_atoms,
                               dP, prec, h->stream));
-  TCW_CUDA(h, launch_map(dT, reinterpret_cast<const WorkItem *>(ws + o_items), n_items, nullptr,
-                         0, false, d_Fmn != nullptr, prec, d_atoms, d_t0s, d_taus, dP, d_Fmn,
-                         dparts, h->stream));
+  MapLaunch ml{};
+  ml.T = dT;
+  ml.items = reinterpret_cast<const WorkItem *>(ws + o_items);
+  ml.n_items = n_items;
+  ml.persistent = false;
+  ml.write_map = d_Fmn != nullptr;
+  ml.prec = prec;
+  ml.priority = h->prio_low;
+  ml.atoms = d_atoms;
+  ml.t0s = d_t0s;
+  ml.taus = d_taus;
+  ml.P = dP;
+  ml.Fmn = d_Fmn;
+  ml.parts = dparts;
+  TCW_CUDA(h, launch_map(window, ml, h->stream));
   TCW_CUDA(h, launch_finalize(dT, 1, dparts, d_result, h->stream));
   if (post)
     TCW_CUDA(h, launch_posteriors(dT, d_Fmn, d_result, reinterpret_cast<double *>(ws + o_row),
@@ -665,14 +697,24 @@ int tcw_plan_create(tcw_handle *h, const tcw_template_desc *desc, uint32_t n_tem
       for (size_t i = first; i < items.size(); i++) items[i].part = (uint32_t)i;
       T[k] = t;
     }
-    // schedule: most expensive tiles first (longest-processing-time order)
+    // two queues (rect tiles, then exp tiles), each in longest-processing-time
+    // order: most expensive tiles first
     std::vector<uint32_t> order(items.size());
     for (size_t i = 0; i < order.size(); i++) order[i] = (uint32_t)i;
-    std::stable_sort(order.begin(), order.end(),
-                     [&](uint32_t a, uint32_t b) { return cost[a] > cost[b]; });
+    auto is_rect = [&](uint32_t i) { return T[items[i].tmpl].window == TCW_WINDOW_RECT; };
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
+      if (is_rect(a) != is_rect(b)) return is_rect(a);
+      return cost[a] > cost[b];
+    });
     std::vector<WorkItem> sorted(items.size());
-    for (size_t i = 0; i < order.size(); i++) sorted[i] = items[order[i]];
+    uint32_t nr = 0;
+    for (size_t i = 0; i < order.size(); i++) {
+      sorted[i] = items[order[i]];
+      if (is_rect(order[i])) nr++;
+    }
     items.swap(sorted);
+    p->n_items_rect = nr;
+    p->n_items_exp = (uint32_t)items.size() - nr;
   } catch (const std::bad_alloc &) {
     delete p;
     return set_err(h, TCW_ERR_ALLOC, "host allocation failed while planning");
@@ -686,8 +728,16 @@ int tcw_plan_create(tcw_handle *h, const tcw_template_desc *desc, uint32_t n_tem
   p->n_cells = cells;
   p->n_atom_rows = atom_rows;
   p->p_rows = p_rows;
-  p->n_blocks = std::max<uint32_t>(1, std::min<uint64_t>(p->n_items,
-                                                         (uint64_t)cfg.blocks_per_sm * h->n_sms));
+  {
+    const uint32_t br = (uint32_t)std::min<int>(map_blocks_per_sm(TCW_WINDOW_RECT, p->prec),
+                                                (int)cfg.blocks_per_sm);
+    const uint32_t be = (uint32_t)std::min<int>(map_blocks_per_sm(TCW_WINDOW_EXP, p->prec),
+                                                (int)cfg.blocks_per_sm);
+    p->n_blocks_rect = (uint32_t)std::max<uint64_t>(
+        1, std::min<uint64_t>(p->n_items_rect, (uint64_t)br * h->n_sms));
+    p->n_blocks_exp = (uint32_t)std::max<uint64_t>(
+        1, std::min<uint64_t>(p->n_items_exp, (uint64_t)be * h->n_sms));
+  }
 
   Layout L;
   const size_t o_T = L.add(sizeof(TemplateDev) * n_templates);
@@ -698,7 +748,7 @@ int tcw_plan_create(tcw_handle *h, const tcw_template_desc *desc, uint32_t n_tem
   const size_t ctl_end = L.total;
   const size_t o_parts = L.add(sizeof(Partial) * p->n_items);
   const size_t o_P = L.add(sizeof(float) * kPrefixStride * std::max<uint64_t>(1, p_rows));
-  const size_t o_cnt = L.add(sizeof(uint32_t));
+  const size_t o_cnt = L.add(2 * sizeof(uint32_t));
   void *buf = nullptr;
   rc = ws_alloc(h, &buf, L.total);
   if (rc) {
@@ -755,13 +805,42 @@ int tcw_plan_info(const tcw_plan *p, uint64_t *n_cells, uint32_t *n_items,
   return TCW_OK;
 }
 
+static MapLaunch plan_launch(const tcw_handle *h, const tcw_plan *p, int window,
+                             const float *d_atoms) {
+  MapLaunch ml{};
+  const bool rect = window == TCW_WINDOW_RECT;
+  ml.T = p->d_T;
+  ml.items = p->d_items + (rect ? 0 : p->n_items_rect);
+  ml.n_items = rect ? p->n_items_rect : p->n_items_exp;
+  ml.counter = p->d_counter + (rect ? 0 : 1);
+  ml.n_blocks = rect ? p->n_blocks_rect : p->n_blocks_exp;
+  ml.persistent = true;
+  ml.write_map = false;
+  ml.prec = p->prec;
+  ml.priority = rect ? h->prio_low : h->prio_high;
+  ml.atoms = d_atoms;
+  ml.t0s = p->d_t0s;
+  ml.taus = p->d_taus;
+  ml.P = p->d_P;
+  ml.Fmn = nullptr;
+  ml.parts = p->d_parts;
+  return ml;
+}
+
+// prefix -> (exp tiles on the main stream at high priority || rect tiles on
+// the side stream) -> finalize.  The exp tiles are the long ones; the rect
+// kernel's blocks fill SMs as exp blocks retire.
 static int plan_enqueue(tcw_handle *h, tcw_plan *p, const float *d_atoms, tcw_result *d_results) {
-  TCW_CUDA(h, cudaMemsetAsync(p->d_counter, 0, sizeof(uint32_t), h->stream));
+  TCW_CUDA(h, cudaMemsetAsync(p->d_counter, 0, 2 * sizeof(uint32_t), h->stream));
   TCW_CUDA(h, launch_prefix(p->d_T, p->d_rect_list, p->n_rect, d_atoms, p->d_P, p->prec,
                             h->stream));
-  TCW_CUDA(h, launch_map(p->d_T, p->d_items, p->n_items, p->d_counter, p->n_blocks, true, false,
-                         p->prec, d_atoms, p->d_t0s, p->d_taus, p->d_P, nullptr, p->d_parts,
-                         h->stream));
+  TCW_CUDA(h, cudaEventRecord(h->fork_ev, h->stream));
+  TCW_CUDA(h, cudaStreamWaitEvent(h->side_stream, h->fork_ev, 0));
+  TCW_CUDA(h, launch_map(TCW_WINDOW_EXP, plan_launch(h, p, TCW_WINDOW_EXP, d_atoms), h->stream));
+  TCW_CUDA(h, launch_map(TCW_WINDOW_RECT, plan_launch(h, p, TCW_WINDOW_RECT, d_atoms),
+                         h->side_stream));
+  TCW_CUDA(h, cudaEventRecord(h->join_ev, h->side_stream));
+  TCW_CUDA(h, cudaStreamWaitEvent(h->stream, h->join_ev, 0));
   TCW_CUDA(h, launch_finalize(p->d_T, p->n_templates, p->d_parts, d_results, h->stream));
   return TCW_OK;
 }
@@ -791,7 +870,7 @@ int tcw_plan_run(tcw_handle *h, tcw_plan *p, const float *d_atoms, tcw_result *d
       return rc;
     }
     if (e != cudaSuccess) return cuda_err(h, e, "cudaStreamEndCapture");
-    e = cudaGraphInstantiate(&p->gexec, graph, 0);
+    e = cudaGraphInstantiate(&p->gexec, graph, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) {
       p->gexec = nullptr;
@@ -811,22 +890,22 @@ int tcw_plan_run_timed(tcw_handle *h, tcw_plan *p, const float *d_atoms, tcw_res
   if (!d_atoms || !d_results) return set_err(h, TCW_ERR_INVALID_ARG, "null device pointer");
   int rc = set_device(h);
   if (rc) return rc;
-  cudaEvent_t ev[4];
-  for (int i = 0; i < 4; i++) TCW_CUDA(h, cudaEventCreate(&ev[i]));
-  TCW_CUDA(h, cudaMemsetAsync(p->d_counter, 0, sizeof(uint32_t), h->stream));
+  cudaEvent_t ev[5];
+  for (int i = 0; i < 5; i++) TCW_CUDA(h, cudaEventCreate(&ev[i]));
+  TCW_CUDA(h, cudaMemsetAsync(p->d_counter, 0, 2 * sizeof(uint32_t), h->stream));
   TCW_CUDA(h, cudaEventRecord(ev[0], h->stream));
   TCW_CUDA(h, launch_prefix(p->d_T, p->d_rect_list, p->n_rect, d_atoms, p->d_P, p->prec,
                             h->stream));
   TCW_CUDA(h, cudaEventRecord(ev[1], h->stream));
-  TCW_CUDA(h, launch_map(p->d_T, p->d_items, p->n_items, p->d_counter, p->n_blocks, true, false,
-                         p->prec, d_atoms, p->d_t0s, p->d_taus, p->d_P, nullptr, p->d_parts,
-                         h->stream));
+  TCW_CUDA(h, launch_map(TCW_WINDOW_RECT, plan_launch(h, p, TCW_WINDOW_RECT, d_atoms), h->stream));
   TCW_CUDA(h, cudaEventRecord(ev[2], h->stream));
-  TCW_CUDA(h, launch_finalize(p->d_T, p->n_templates, p->d_parts, d_results, h->stream));
+  TCW_CUDA(h, launch_map(TCW_WINDOW_EXP, plan_launch(h, p, TCW_WINDOW_EXP, d_atoms), h->stream));
   TCW_CUDA(h, cudaEventRecord(ev[3], h->stream));
-  TCW_CUDA(h, cudaEventSynchronize(ev[3]));
-  for (int i = 0; i < 3; i++) TCW_CUDA(h, cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]));
-  for (int i = 0; i < 4; i++) cudaEventDestroy(ev[i]);
+  TCW_CUDA(h, launch_finalize(p->d_T, p->n_templates, p->d_parts, d_results, h->stream));
+  TCW_CUDA(h, cudaEventRecord(ev[4], h->stream));
+  TCW_CUDA(h, cudaEventSynchronize(ev[4]));
+  for (int i = 0; i < 4; i++) TCW_CUDA(h, cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]));
+  for (int i = 0; i < 5; i++) cudaEventDestroy(ev[i]);
   return TCW_OK;
 }
 

@@ -58,11 +58,25 @@ struct Partial {
 // Launchers (tcw_kernels.cu).  All asynchronous on `stream`.
 cudaError_t launch_prefix(const TemplateDev *d_T, const uint32_t *d_rect_list, uint32_t n_rect,
                           const float *d_atoms, float *d_P, int prec, cudaStream_t stream);
-cudaError_t launch_map(const TemplateDev *d_T, const WorkItem *d_items, uint32_t n_items,
-                       uint32_t *d_counter, uint32_t n_blocks, bool persistent, bool write_map,
-                       int prec, const float *d_atoms, const uint32_t *d_t0s,
-                       const uint32_t *d_taus, const float *d_P, float *d_Fmn, Partial *d_parts,
-                       cudaStream_t stream);
+struct MapLaunch {
+  const TemplateDev *T;
+  const WorkItem *items;  // this window's tiles
+  uint32_t n_items;
+  uint32_t *counter;      // persistent launches: tile counter, zeroed before
+  uint32_t n_blocks;      // persistent grid size
+  bool persistent, write_map;
+  int prec;
+  int priority;           // stream-priority value of the launch
+  const float *atoms;
+  const uint32_t *t0s, *taus;
+  const float *P;
+  float *Fmn;
+  Partial *parts;
+};
+cudaError_t launch_map(int window, const MapLaunch &L, cudaStream_t stream);
+// Resident blocks per SM of the persistent (map-less) kernel of a window.
+int map_blocks_per_sm(int window, int prec);
+
 cudaError_t launch_finalize(const TemplateDev *d_T, uint32_t n_templates, const Partial *d_parts,
                             void *d_results, cudaStream_t stream);
 cudaError_t launch_posteriors(const TemplateDev *d_T, const float *d_Fmn, void *d_result,

@@ -232,32 +232,13 @@ __device__ void block_reduce_store(const Red &red, Partial *out) {
 
 // ------------------------------------------------------------------ tiles
 
-template <int kPrec>
-__device__ __forceinline__ float rect_cell_dev(const float *P, const float *row0, uint32_t j0,
-                                               uint32_t e, bool &ok) {
-  if (e < j0) {
-    ok = false;
-    return 2.0f;
-  }
-  float r1[16];
-  ld_row16(P + (size_t)(e + 1u) * kPrefixStride, r1);
-  FF W[7];
-#pragma unroll
-  for (int c = 0; c < 7; c++) {
-    W[c].h = fsub(r1[c], row0[c]);
-    W[c].l = fsub(r1[8 + c], row0[8 + c]);
-  }
-  if (kPrec == kPrecPlain32)
-    return fstat_plain32(W[0].h, W[1].h, W[2].h, W[3].h, W[4].h, W[5].h, W[6].h, ok);
-  return fstat_tiered<kPrec == kPrecFF_F64Det>(W, ok);
-}
-
 // Rectangular tile: each thread owns one row (t0) and walks the tile's
 // columns, so the row's start index, its prefix row and the u32-wrap state
 // are set up once per row; per cell only the end index and one prefix row
-// are needed.  The block's 4 warps are (rg row groups of 32 rows) x (4/rg
-// column ranges).  With a map to write, each warp transposes 32 x 32 blocks
-// through shared memory so that global stores are row-contiguous.
+// are needed, and the next cell's prefix row is loaded while the current
+// cell is computed.  The block's 4 warps are (rg row groups of 32 rows) x
+// (4/rg column ranges).  With a map to write, each warp transposes 32 x 32
+// blocks through shared memory so that global stores are row-contiguous.
 template <bool kWrite, int kPrec>
 __device__ void rect_tile(const TemplateDev &t, const WorkItem &w,
                           const uint32_t *__restrict__ t0s_all,
@@ -287,20 +268,48 @@ __device__ void rect_tile(const TemplateDev &t, const WorkItem &w,
     ef = wr ? idx_end(t0 + tau_first, t.g) : 0u;
     ld_row16(P + (size_t)j0 * kPrefixStride, row0);
   }
+  auto end_of = [&](uint32_t n) {
+    uint32_t e = idx_end(t0 + __ldg(taus + n), t.g);
+    return (wr && ef > e) ? ef : e;
+  };
+  // e < numAtoms always, so prefix row e + 1 exists even for empty windows
+  uint32_t e_cur = 0;
+  float cur[16];
+  if (row_ok && nb < ne) {
+    e_cur = end_of(nb);
+    ld_row16(P + (size_t)(e_cur + 1u) * kPrefixStride, cur);
+  }
   const int64_t rowidx = (int64_t)m * t.N_tau;
   for (uint32_t cb = nb; cb < ne; cb += 32u) {
     const uint32_t ce = min(ne, cb + 32u);
     for (uint32_t n = cb; n < ce; n++) {
-      const uint32_t tau = __ldg(taus + n);
+      uint32_t e_nxt = 0;
+      float nxt[16];
+      if (row_ok && n + 1u < ne) {
+        e_nxt = end_of(n + 1u);
+        ld_row16(P + (size_t)(e_nxt + 1u) * kPrefixStride, nxt);
+      }
       float F = 2.0f;
       if (row_ok) {
-        uint32_t e = idx_end(t0 + tau, t.g);
-        if (wr && ef > e) e = ef;
-        bool ok;
-        F = rect_cell_dev<kPrec>(P, row0, j0, e, ok);
+        if (e_cur >= j0) {
+          FF W[7];
+#pragma unroll
+          for (int c = 0; c < 7; c++) {
+            W[c].h = fsub(cur[c], row0[c]);
+            W[c].l = fsub(cur[8 + c], row0[8 + c]);
+          }
+          bool ok;
+          if (kPrec == kPrecPlain32)
+            F = fstat_plain32(W[0].h, W[1].h, W[2].h, W[3].h, W[4].h, W[5].h, W[6].h, ok);
+          else
+            F = fstat_tiered<kPrec == kPrecFF_F64Det>(W, ok);
+        }
         red.add(F, rowidx + n);
       }
       if (kWrite) smw[lane * 33u + (n - cb)] = F;
+#pragma unroll
+      for (int k = 0; k < 16; k++) cur[k] = nxt[k];
+      e_cur = e_nxt;
     }
     if (kWrite) {
       __syncwarp();
@@ -364,7 +373,7 @@ __device__ void exp_tile(const TemplateDev &t, const WorkItem &w, const float *_
   }
 }
 
-template <bool kPersist, bool kWrite, int kPrec>
+template <int kWin, bool kPersist, bool kWrite, int kPrec>
 __global__ void __launch_bounds__(kBlock)
     map_kernel(const TemplateDev *__restrict__ T, const WorkItem *__restrict__ items,
                uint32_t n_items, uint32_t *__restrict__ counter, const float *__restrict__ atoms,
@@ -372,10 +381,9 @@ __global__ void __launch_bounds__(kBlock)
                const float *__restrict__ P, float *__restrict__ Fmn,
                Partial *__restrict__ parts) {
   __shared__ uint32_t s_item;
-  __shared__ union {
-    float warp_tile[kBlock / 32][32 * 33];  // rect map-write transposes
-    uint32_t lo[kExpLoTab];                 // exp window starts
-  } sm;
+  constexpr uint32_t kSmem = kWin == TCW_WINDOW_RECT ? (kWrite ? (kBlock / 32) * 32 * 33 : 1)
+                                                     : kExpLoTab;
+  __shared__ __align__(16) uint32_t sm[kSmem];
   uint32_t it = blockIdx.x;
   for (;;) {
     if (kPersist) {
@@ -389,10 +397,11 @@ __global__ void __launch_bounds__(kBlock)
     const TemplateDev t = T[w.tmpl];
     Red red;
     red.init();
-    if (t.window == TCW_WINDOW_RECT)
-      rect_tile<kWrite, kPrec>(t, w, t0s, taus, P, Fmn, red, sm.warp_tile[threadIdx.x >> 5]);
+    if (kWin == TCW_WINDOW_RECT)
+      rect_tile<kWrite, kPrec>(t, w, t0s, taus, P, Fmn, red,
+                               reinterpret_cast<float *>(sm) + (threadIdx.x >> 5) * (32 * 33));
     else
-      exp_tile<kWrite, kPrec>(t, w, atoms, t0s, taus, Fmn, red, sm.lo);
+      exp_tile<kWrite, kPrec>(t, w, atoms, t0s, taus, Fmn, red, sm);
     block_reduce_store(red, parts + w.part);
     if (!kPersist) break;
   }
@@ -562,44 +571,84 @@ cudaError_t launch_prefix(const TemplateDev *d_T, const uint32_t *d_rect_list, u
   return cudaGetLastError();
 }
 
-template <bool kPersist, bool kWrite>
-static void launch_map_prec(int prec, uint32_t grid, cudaStream_t s, const TemplateDev *T,
-                            const WorkItem *items, uint32_t n_items, uint32_t *counter,
-                            const float *atoms, const uint32_t *t0s, const uint32_t *taus,
-                            const float *P, float *Fmn, Partial *parts) {
+template <int kWin, bool kPersist, bool kWrite>
+static cudaError_t launch_map_prec(int prec, uint32_t grid, cudaStream_t s, int priority,
+                                   const TemplateDev *T, const WorkItem *items, uint32_t n_items,
+                                   uint32_t *counter, const float *atoms, const uint32_t *t0s,
+                                   const uint32_t *taus, const float *P, float *Fmn,
+                                   Partial *parts) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(kBlock);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributePriority;
+  attr[0].val.priority = priority;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
   if (prec == kPrecPlain32)
-    map_kernel<kPersist, kWrite, kPrecPlain32>
-        <<<grid, kBlock, 0, s>>>(T, items, n_items, counter, atoms, t0s, taus, P, Fmn, parts);
-  else if (prec == kPrecFF_F64Det)
-    map_kernel<kPersist, kWrite, kPrecFF_F64Det>
-        <<<grid, kBlock, 0, s>>>(T, items, n_items, counter, atoms, t0s, taus, P, Fmn, parts);
-  else
-    map_kernel<kPersist, kWrite, kPrecFF>
-        <<<grid, kBlock, 0, s>>>(T, items, n_items, counter, atoms, t0s, taus, P, Fmn, parts);
+    return cudaLaunchKernelEx(&cfg, map_kernel<kWin, kPersist, kWrite, kPrecPlain32>, T, items,
+                              n_items, counter, atoms, t0s, taus, P, Fmn, parts);
+  if (prec == kPrecFF_F64Det)
+    return cudaLaunchKernelEx(&cfg, map_kernel<kWin, kPersist, kWrite, kPrecFF_F64Det>, T, items,
+                              n_items, counter, atoms, t0s, taus, P, Fmn, parts);
+  return cudaLaunchKernelEx(&cfg, map_kernel<kWin, kPersist, kWrite, kPrecFF>, T, items, n_items,
+                            counter, atoms, t0s, taus, P, Fmn, parts);
 }
 
-cudaError_t launch_map(const TemplateDev *d_T, const WorkItem *d_items, uint32_t n_items,
-                       uint32_t *d_counter, uint32_t n_blocks, bool persistent, bool write_map,
-                       int prec, const float *d_atoms, const uint32_t *d_t0s,
-                       const uint32_t *d_taus, const float *d_P, float *d_Fmn, Partial *d_parts,
-                       cudaStream_t stream) {
-  if (n_items == 0) return cudaSuccess;
-  if (persistent) {
-    if (write_map)
-      launch_map_prec<true, true>(prec, n_blocks, stream, d_T, d_items, n_items, d_counter,
-                                  d_atoms, d_t0s, d_taus, d_P, d_Fmn, d_parts);
-    else
-      launch_map_prec<true, false>(prec, n_blocks, stream, d_T, d_items, n_items, d_counter,
-                                   d_atoms, d_t0s, d_taus, d_P, d_Fmn, d_parts);
-  } else {
-    if (write_map)
-      launch_map_prec<false, true>(prec, n_items, stream, d_T, d_items, n_items, d_counter,
-                                   d_atoms, d_t0s, d_taus, d_P, d_Fmn, d_parts);
-    else
-      launch_map_prec<false, false>(prec, n_items, stream, d_T, d_items, n_items, d_counter,
-                                    d_atoms, d_t0s, d_taus, d_P, d_Fmn, d_parts);
+template <int kWin>
+static cudaError_t launch_map_win(const MapLaunch &L, cudaStream_t stream) {
+  if (L.n_items == 0) return cudaSuccess;
+  const uint32_t grid = L.persistent ? L.n_blocks : L.n_items;
+  if (L.persistent) {
+    if (L.write_map)
+      return launch_map_prec<kWin, true, true>(L.prec, grid, stream, L.priority, L.T, L.items,
+                                               L.n_items, L.counter, L.atoms, L.t0s, L.taus, L.P,
+                                               L.Fmn, L.parts);
+    return launch_map_prec<kWin, true, false>(L.prec, grid, stream, L.priority, L.T, L.items,
+                                              L.n_items, L.counter, L.atoms, L.t0s, L.taus, L.P,
+                                              L.Fmn, L.parts);
   }
+  if (L.write_map)
+    return launch_map_prec<kWin, false, true>(L.prec, grid, stream, L.priority, L.T, L.items,
+                                              L.n_items, L.counter, L.atoms, L.t0s, L.taus, L.P,
+                                              L.Fmn, L.parts);
+  return launch_map_prec<kWin, false, false>(L.prec, grid, stream, L.priority, L.T, L.items,
+                                             L.n_items, L.counter, L.atoms, L.t0s, L.taus, L.P,
+                                             L.Fmn, L.parts);
+}
+
+cudaError_t launch_map(int window, const MapLaunch &L, cudaStream_t stream) {
+  cudaError_t e = window == TCW_WINDOW_RECT ? launch_map_win<TCW_WINDOW_RECT>(L, stream)
+                                            : launch_map_win<TCW_WINDOW_EXP>(L, stream);
+  if (e != cudaSuccess) return e;
   return cudaGetLastError();
+}
+
+template <int kWin>
+static int blocks_per_sm_win(int prec) {
+  int n = 0;
+  cudaError_t e;
+  if (prec == kPrecPlain32)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &n, map_kernel<kWin, true, false, kPrecPlain32>, kBlock, 0);
+  else if (prec == kPrecFF_F64Det)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &n, map_kernel<kWin, true, false, kPrecFF_F64Det>, kBlock, 0);
+  else
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, map_kernel<kWin, true, false, kPrecFF>,
+                                                      kBlock, 0);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    n = 1;
+  }
+  return n > 0 ? n : 1;
+}
+
+// Resident blocks per SM of the persistent (map-less) kernel of a window.
+int map_blocks_per_sm(int window, int prec) {
+  return window == TCW_WINDOW_RECT ? blocks_per_sm_win<TCW_WINDOW_RECT>(prec)
+                                   : blocks_per_sm_win<TCW_WINDOW_EXP>(prec);
 }
 
 cudaError_t launch_finalize(const TemplateDev *d_T, uint32_t n_templates, const Partial *d_parts,
