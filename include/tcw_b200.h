@@ -151,9 +151,11 @@ int tcw_plan_run_timed(tcw_handle *h, tcw_plan *plan, const float *d_atoms, tcw_
                        float *ms);
 
 /* Measured throughput of `device` for roofline denominators: FP32 and FP64
- * FMA in TFLOP/s (an FMA counts 2) and MUFU ex2 in Tops/s.  A measurement
- * utility; it has no counterpart in the reference. */
-int tcw_probe_peaks(int device, double *fp32_tflops, double *fp64_tflops, double *mufu_tops);
+ * FMA in TFLOP/s (an FMA counts 2), MUFU ex2 in Tops/s, FP32 through packed
+ * f32x2 FMAs in TFLOP/s.  A measurement utility; it has no counterpart in the
+ * reference. */
+int tcw_probe_peaks(int device, double *fp32_tflops, double *fp64_tflops, double *mufu_tops,
+                    double *fp32x2_tflops);
 
 /* Test hook: make the n-th following workspace allocation on this handle
  * fail (n = 0 disables).  Host-side only; used to test error paths. */

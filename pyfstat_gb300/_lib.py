@@ -94,6 +94,7 @@ SIGNATURES = {
     "tcw_debug_fail_alloc": (ctypes.c_int, [_vp, ctypes.c_int]),
     "tcw_probe_peaks": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                        ctypes.POINTER(ctypes.c_double),
+                                       ctypes.POINTER(ctypes.c_double),
                                        ctypes.POINTER(ctypes.c_double)]),
 }
 
@@ -158,10 +159,12 @@ def device_info(device):
 
 
 def probe_peaks(device=0):
-    """Measured FP32 / FP64 TFLOP/s and MUFU ex2 Tops/s of ``device``."""
-    a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
-    check(load().tcw_probe_peaks(int(device), ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
-    return dict(fp32_tflops=a.value, fp64_tflops=b.value, mufu_tops=c.value)
+    """Measured FP32 / FP64 / packed-FP32x2 TFLOP/s and MUFU ex2 Tops/s of ``device``."""
+    a, b, c, d = ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    check(load().tcw_probe_peaks(int(device), ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
+                                 ctypes.byref(d)))
+    return dict(fp32_tflops=a.value, fp64_tflops=b.value, mufu_tops=c.value,
+                fp32x2_tflops=d.value)
 
 
 def _ptr(a):

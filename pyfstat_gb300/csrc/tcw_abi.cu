@@ -50,7 +50,9 @@ struct tcw_plan {
   TemplateDev *d_T = nullptr;
   WorkItem *d_items = nullptr;
   Partial *d_parts = nullptr;
-  uint32_t *d_rect_list = nullptr, *d_t0s = nullptr, *d_taus = nullptr;
+  uint32_t *d_rect_list = nullptr, *d_exp_list = nullptr, *d_t0s = nullptr, *d_taus = nullptr;
+  uint32_t n_exp = 0;
+  float *d_A8 = nullptr;  // exp templates' atoms in rows of 8 floats
   uint32_t *d_counter = nullptr;  // [0] rect tiles, [1] exp tiles
   float *d_P = nullptr;
   // graph state
@@ -467,12 +469,15 @@ static int plain_enqueue(tcw_handle *h, const float *d_atoms, uint32_t numAtoms,
   Layout L;
   L.total = ws_off;
   const size_t o_T = L.add(sizeof(TemplateDev));
-  const size_t o_list = L.add(sizeof(uint32_t));
+  const size_t o_list = L.add(sizeof(uint32_t));  // {0}: the one template
   const size_t o_items = L.add(sizeof(WorkItem) * n_items);
   const size_t o_parts = L.add(sizeof(Partial) * n_items);
   const size_t o_P = window == TCW_WINDOW_RECT
                          ? L.add(sizeof(float) * kPrefixStride * ((size_t)numAtoms + 1))
                          : 0;
+  const size_t o_A8 = window == TCW_WINDOW_EXP
+                          ? L.add(sizeof(float) * 8u * (size_t)numAtoms)
+                          : 0;
   const size_t o_row = post ? L.add(sizeof(double) * N_t0) : 0;
   const size_t o_col = post ? L.add(sizeof(double) * (size_t)n_chunks * N_tau) : 0;
   int rc = ensure_ws(h, L.total);
@@ -497,6 +502,10 @@ static int plain_enqueue(tcw_handle *h, const float *d_atoms, uint32_t numAtoms,
   if (window == TCW_WINDOW_RECT)
     TCW_CUDA(h, launch_prefix(dT, reinterpret_cast<const uint32_t *>(ws + o_list), 1, d_atoms,
                               dP, prec, h->stream));
+  float *dA8 = window == TCW_WINDOW_EXP ? reinterpret_cast<float *>(ws + o_A8) : nullptr;
+  if (window == TCW_WINDOW_EXP)
+    TCW_CUDA(h, launch_repack(dT, reinterpret_cast<const uint32_t *>(ws + o_list), 1, d_atoms,
+                              dA8, h->stream));
   MapLaunch ml{};
   ml.T = dT;
   ml.items = reinterpret_cast<const WorkItem *>(ws + o_items);
@@ -506,6 +515,7 @@ static int plain_enqueue(tcw_handle *h, const float *d_atoms, uint32_t numAtoms,
   ml.prec = prec;
   ml.priority = h->prio_low;
   ml.atoms = d_atoms;
+  ml.atoms8 = dA8;
   ml.t0s = d_t0s;
   ml.taus = d_taus;
   ml.P = dP;
@@ -597,6 +607,7 @@ int tcw_map_plain_host(tcw_handle *h, const float *atoms, uint32_t numAtoms, uin
     L2.add(sizeof(WorkItem) * items_est);
     L2.add(sizeof(Partial) * items_est);
     if (window == TCW_WINDOW_RECT) L2.add(sizeof(float) * kPrefixStride * ((size_t)numAtoms + 1));
+    if (window == TCW_WINDOW_EXP) L2.add(sizeof(float) * 8u * (size_t)numAtoms);
     L2.add(sizeof(double) * N_t0);
     L2.add(sizeof(double) * ((N_t0 + 63u) / 64u) * (size_t)N_tau);
     need_after = L2.total;
@@ -655,8 +666,8 @@ int tcw_plan_create(tcw_handle *h, const tcw_template_desc *desc, uint32_t n_tem
   std::vector<TemplateDev> T(n_templates);
   std::vector<WorkItem> items;
   std::vector<double> cost;
-  std::vector<uint32_t> rect_list;
-  uint64_t p_rows = 0, atom_rows = 0, cells = 0;
+  std::vector<uint32_t> rect_list, exp_list;
+  uint64_t p_rows = 0, a8_rows = 0, atom_rows = 0, cells = 0;
   try {
     for (uint32_t k = 0; k < n_templates; k++) {
       const tcw_template_desc &d = desc[k];
@@ -687,6 +698,10 @@ int tcw_plan_create(tcw_handle *h, const tcw_template_desc *desc, uint32_t n_tem
         t.p_off = p_rows;
         p_rows += (uint64_t)d.numAtoms + 1u;
         rect_list.push_back(k);
+      } else {
+        t.a8_off = a8_rows;
+        a8_rows += d.numAtoms;
+        exp_list.push_back(k);
       }
       atom_rows = std::max<uint64_t>(atom_rows, d.atom_offset + d.numAtoms);
       cells += (uint64_t)d.N_t0 * d.N_tau;
@@ -725,6 +740,7 @@ int tcw_plan_create(tcw_handle *h, const tcw_template_desc *desc, uint32_t n_tem
   }
   p->n_items = (uint32_t)items.size();
   p->n_rect = (uint32_t)rect_list.size();
+  p->n_exp = (uint32_t)exp_list.size();
   p->n_cells = cells;
   p->n_atom_rows = atom_rows;
   p->p_rows = p_rows;
@@ -743,11 +759,13 @@ int tcw_plan_create(tcw_handle *h, const tcw_template_desc *desc, uint32_t n_tem
   const size_t o_T = L.add(sizeof(TemplateDev) * n_templates);
   const size_t o_items = L.add(sizeof(WorkItem) * p->n_items);
   const size_t o_list = L.add(sizeof(uint32_t) * std::max<size_t>(1, rect_list.size()));
+  const size_t o_elist = L.add(sizeof(uint32_t) * std::max<size_t>(1, exp_list.size()));
   const size_t o_t0 = L.add(sizeof(uint32_t) * n_t0s);
   const size_t o_tau = L.add(sizeof(uint32_t) * n_taus);
   const size_t ctl_end = L.total;
   const size_t o_parts = L.add(sizeof(Partial) * p->n_items);
   const size_t o_P = L.add(sizeof(float) * kPrefixStride * std::max<uint64_t>(1, p_rows));
+  const size_t o_A8 = L.add(sizeof(float) * 8u * std::max<uint64_t>(1, a8_rows));
   const size_t o_cnt = L.add(2 * sizeof(uint32_t));
   void *buf = nullptr;
   rc = ws_alloc(h, &buf, L.total);
@@ -759,6 +777,8 @@ int tcw_plan_create(tcw_handle *h, const tcw_template_desc *desc, uint32_t n_tem
   p->d_T = reinterpret_cast<TemplateDev *>(p->d_buf + o_T);
   p->d_items = reinterpret_cast<WorkItem *>(p->d_buf + o_items);
   p->d_rect_list = reinterpret_cast<uint32_t *>(p->d_buf + o_list);
+  p->d_exp_list = reinterpret_cast<uint32_t *>(p->d_buf + o_elist);
+  p->d_A8 = reinterpret_cast<float *>(p->d_buf + o_A8);
   p->d_t0s = reinterpret_cast<uint32_t *>(p->d_buf + o_t0);
   p->d_taus = reinterpret_cast<uint32_t *>(p->d_buf + o_tau);
   p->d_parts = reinterpret_cast<Partial *>(p->d_buf + o_parts);
@@ -770,6 +790,8 @@ int tcw_plan_create(tcw_handle *h, const tcw_template_desc *desc, uint32_t n_tem
   memcpy(host.data() + o_items, items.data(), sizeof(WorkItem) * p->n_items);
   if (!rect_list.empty())
     memcpy(host.data() + o_list, rect_list.data(), sizeof(uint32_t) * rect_list.size());
+  if (!exp_list.empty())
+    memcpy(host.data() + o_elist, exp_list.data(), sizeof(uint32_t) * exp_list.size());
   memcpy(host.data() + o_t0, t0s, sizeof(uint32_t) * n_t0s);
   memcpy(host.data() + o_tau, taus, sizeof(uint32_t) * n_taus);
   cudaError_t e = cudaMemcpy(p->d_buf, host.data(), ctl_end, cudaMemcpyHostToDevice);
@@ -819,6 +841,7 @@ static MapLaunch plan_launch(const tcw_handle *h, const tcw_plan *p, int window,
   ml.prec = p->prec;
   ml.priority = rect ? h->prio_low : h->prio_high;
   ml.atoms = d_atoms;
+  ml.atoms8 = p->d_A8;
   ml.t0s = p->d_t0s;
   ml.taus = p->d_taus;
   ml.P = p->d_P;
@@ -836,6 +859,7 @@ static int plan_enqueue(tcw_handle *h, tcw_plan *p, const float *d_atoms, tcw_re
                             h->stream));
   TCW_CUDA(h, cudaEventRecord(h->fork_ev, h->stream));
   TCW_CUDA(h, cudaStreamWaitEvent(h->side_stream, h->fork_ev, 0));
+  TCW_CUDA(h, launch_repack(p->d_T, p->d_exp_list, p->n_exp, d_atoms, p->d_A8, h->stream));
   TCW_CUDA(h, launch_map(TCW_WINDOW_EXP, plan_launch(h, p, TCW_WINDOW_EXP, d_atoms), h->stream));
   TCW_CUDA(h, launch_map(TCW_WINDOW_RECT, plan_launch(h, p, TCW_WINDOW_RECT, d_atoms),
                          h->side_stream));
@@ -896,6 +920,7 @@ int tcw_plan_run_timed(tcw_handle *h, tcw_plan *p, const float *d_atoms, tcw_res
   TCW_CUDA(h, cudaEventRecord(ev[0], h->stream));
   TCW_CUDA(h, launch_prefix(p->d_T, p->d_rect_list, p->n_rect, d_atoms, p->d_P, p->prec,
                             h->stream));
+  TCW_CUDA(h, launch_repack(p->d_T, p->d_exp_list, p->n_exp, d_atoms, p->d_A8, h->stream));
   TCW_CUDA(h, cudaEventRecord(ev[1], h->stream));
   TCW_CUDA(h, launch_map(TCW_WINDOW_RECT, plan_launch(h, p, TCW_WINDOW_RECT, d_atoms), h->stream));
   TCW_CUDA(h, cudaEventRecord(ev[2], h->stream));

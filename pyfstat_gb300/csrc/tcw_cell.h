@@ -110,6 +110,83 @@ TCW_HD float ex2_approx(float x) {
 #endif
 }
 
+// ------------------------------------------------------------ packed pairs
+// Two FP32 lanes operated on together.  On the device these are the packed
+// add/sub/mul/fma.rn.f32x2 instructions (one issue slot for two results);
+// the host build does the same two IEEE operations one after the other, so
+// both give identical results.
+struct F2 {
+  float x, y;
+};
+
+#if defined(__CUDA_ARCH__)
+__device__ __forceinline__ unsigned long long f2_pack(F2 a) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+  return r;
+}
+__device__ __forceinline__ F2 f2_unpack(unsigned long long v) {
+  F2 r;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+  return r;
+}
+#endif
+
+TCW_HD F2 add2(F2 a, F2 b) {
+#if defined(__CUDA_ARCH__)
+  unsigned long long r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_pack(a)), "l"(f2_pack(b)));
+  return f2_unpack(r);
+#else
+  return F2{a.x + b.x, a.y + b.y};
+#endif
+}
+TCW_HD F2 sub2(F2 a, F2 b) {
+#if defined(__CUDA_ARCH__)
+  unsigned long long r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_pack(a)), "l"(f2_pack(b)));
+  return f2_unpack(r);
+#else
+  return F2{a.x - b.x, a.y - b.y};
+#endif
+}
+TCW_HD F2 mul2(F2 a, F2 b) {
+#if defined(__CUDA_ARCH__)
+  unsigned long long r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_pack(a)), "l"(f2_pack(b)));
+  return f2_unpack(r);
+#else
+  return F2{a.x * b.x, a.y * b.y};
+#endif
+}
+TCW_HD F2 fma2(F2 a, F2 b, F2 c) {
+#if defined(__CUDA_ARCH__)
+  unsigned long long r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(f2_pack(a)), "l"(f2_pack(b)),
+      "l"(f2_pack(c)));
+  return f2_unpack(r);
+#else
+  return F2{fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y)};
+#endif
+}
+
+// Double-word pair: hi and lo words of two channels.
+struct FF2 {
+  F2 h, l;
+};
+
+// x + r*E for two channels at once (ff_axpy per lane).  nrh = -r.h.
+TCW_HD FF2 ff2_axpy(F2 x, F2 rh, F2 nrh, F2 rl, FF2 E) {
+  const F2 q = mul2(nrh, E.h);        // -p, p = fl(r.h E.h)
+  F2 pe = fma2(rh, E.h, q);           // exact product error
+  pe = fma2(rh, E.l, pe);
+  pe = fma2(rl, E.h, pe);
+  const F2 s = sub2(x, q);            // x + p
+  const F2 bb = sub2(s, x);
+  const F2 e = sub2(sub2(x, sub2(s, bb)), add2(q, bb));  // TwoSum error of x + p
+  return FF2{s, add2(e, pe)};
+}
+
 // Unevaluated sum hi + lo.
 struct FF {
   float h, l;
@@ -333,22 +410,51 @@ TCW_HD float fstat_ff(FF A, FF B, FF C, FF Far, FF Fai, FF Fbr, FF Fbi, bool &ok
 // F) when the cell needs tier 2 (fstat_ff on the double-word sums).
 constexpr float kFastCond = 32.0f;
 
-TCW_HD bool fstat_fast(const FF W[7], float &F) {
-  const float A = fadd(W[0].h, W[0].l);
-  const float B = fadd(W[1].h, W[1].l);
-  const float C = fadd(W[2].h, W[2].l);
+TCW_HD bool fstat_fast_sums(float A, float B, float C, float Far, float Fai, float Fbr,
+                            float Fbi, float &F) {
   const float D = ffma(A, B, -fmul(C, C));
   const float dAB = fsub(A, B);
   const float disc = sqrt_approx(ffma(dAB, dAB, fmul(4.0f * C, C)));
   const float t = fadd(fadd(A, B), disc);
   if (!(fmul(t, t) < fmul(4.0f * kFastCond, D))) return false;
-  const float Far = fadd(W[3].h, W[3].l), Fai = fadd(W[4].h, W[4].l);
-  const float Fbr = fadd(W[5].h, W[5].l), Fbi = fadd(W[6].h, W[6].l);
   const float Gre = ffma(B, Far, -fmul(C, Fbr));
   const float Gim = ffma(B, Fai, -fmul(C, Fbi));
   const float num = ffma(D, ffma(Fbr, Fbr, fmul(Fbi, Fbi)), ffma(Gre, Gre, fmul(Gim, Gim)));
   F = div_approx(num, fmul(B, D));
   return true;
+}
+
+TCW_HD bool fstat_fast(const FF W[7], float &F) {
+  return fstat_fast_sums(fadd(W[0].h, W[0].l), fadd(W[1].h, W[1].l), fadd(W[2].h, W[2].l),
+                         fadd(W[3].h, W[3].l), fadd(W[4].h, W[4].l), fadd(W[5].h, W[5].l),
+                         fadd(W[6].h, W[6].l), F);
+}
+
+// Window sums held as four channel pairs (A,B) (C,Fa_re) (Fa_im,Fb_re)
+// (Fb_im,-): unpack to seven double-words.
+TCW_HD void ff2_unpack(const FF2 P[4], FF W[7]) {
+  W[0] = FF{P[0].h.x, P[0].l.x};
+  W[1] = FF{P[0].h.y, P[0].l.y};
+  W[2] = FF{P[1].h.x, P[1].l.x};
+  W[3] = FF{P[1].h.y, P[1].l.y};
+  W[4] = FF{P[2].h.x, P[2].l.x};
+  W[5] = FF{P[2].h.y, P[2].l.y};
+  W[6] = FF{P[3].h.x, P[3].l.x};
+}
+
+// Tier 1 from paired sums (one packed add per pair), tier 2 otherwise.
+template <bool kFp64Det>
+TCW_HD float fstat_tiered2(const FF2 P[4], bool &ok) {
+  const F2 s0 = add2(P[0].h, P[0].l), s1 = add2(P[1].h, P[1].l);
+  const F2 s2 = add2(P[2].h, P[2].l), s3 = add2(P[3].h, P[3].l);
+  float F;
+  if (fstat_fast_sums(s0.x, s0.y, s1.x, s1.y, s2.x, s2.y, s3.x, F)) {
+    ok = true;
+    return F;
+  }
+  FF W[7];
+  ff2_unpack(P, W);
+  return fstat_ff<kFp64Det>(W[0], W[1], W[2], W[3], W[4], W[5], W[6], ok);
 }
 
 // Both tiers for double-word window sums that are exact enough for tier 2.
@@ -441,9 +547,16 @@ TCW_HD float rect_cell(const float *P, const float *P0, uint32_t j0, uint32_t e,
     return 2.0f;
   }
   const float *P1 = P + (size_t)(e + 1u) * kPrefixStride;
+  if (kComp) {
+    FF2 W[4];
+    for (int k = 0; k < 4; k++) {
+      W[k].h = sub2(F2{P1[2 * k], P1[2 * k + 1]}, F2{P0[2 * k], P0[2 * k + 1]});
+      W[k].l = sub2(F2{P1[8 + 2 * k], P1[9 + 2 * k]}, F2{P0[8 + 2 * k], P0[9 + 2 * k]});
+    }
+    return fstat_tiered2<kFp64Det>(W, ok);
+  }
   FF W[7];
   rect_window_sums(P0, P1, W);
-  if (kComp) return fstat_tiered<kFp64Det>(W, ok);
   return fstat_plain32(W[0].h, W[1].h, W[2].h, W[3].h, W[4].h, W[5].h, W[6].h, ok);
 }
 
@@ -659,6 +772,159 @@ TCW_HD void exp_column(const float *__restrict__ atoms, const Geom &g,
 #pragma unroll
         for (int c = 3; c < 7; c++) W[c] = ff_sub_scaled2(Elo[c], pw, Ehi[c]);
         F = fstat_ff<kFp64Det>(W[0], W[1], W[2], W[3], W[4], W[5], W[6], ok);
+      }
+    }
+    sink(m, F, ok);
+  }
+}
+
+// ------------------------------------------------------------ packed exponential column
+// The same column walk as exp_column with the seven channels in four packed
+// pairs and the atoms in 32-byte rows [a2 b2 ab Fa_re Fa_im Fb_re Fb_im 0]
+// (one 256-bit load per recurrence step on the device).  Pair k of the
+// state runs with the pair of ratios (r2 r2) (r2 r1) (r1 r1) (r1 0).
+TCW_HD void load_row8(const float *__restrict__ p, F2 x[4]) {
+#if defined(__CUDA_ARCH__)
+  asm volatile("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=f"(x[0].x), "=f"(x[0].y), "=f"(x[1].x), "=f"(x[1].y), "=f"(x[2].x),
+                 "=f"(x[2].y), "=f"(x[3].x), "=f"(x[3].y)
+               : "l"(p));
+#else
+  for (int k = 0; k < 4; k++) x[k] = F2{p[2 * k], p[2 * k + 1]};
+#endif
+}
+
+struct ExpConsts2 {
+  F2 rh[4], nrh[4], rl[4];
+};
+
+TCW_HD ExpConsts2 exp_consts2(const ExpConsts &k) {
+  ExpConsts2 c;
+  const FF r[4][2] = {{k.r2, k.r2}, {k.r2, k.r1}, {k.r1, k.r1}, {k.r1, FF{0.0f, 0.0f}}};
+  for (int i = 0; i < 4; i++) {
+    c.rh[i] = F2{r[i][0].h, r[i][1].h};
+    c.nrh[i] = F2{-r[i][0].h, -r[i][1].h};
+    c.rl[i] = F2{r[i][0].l, r[i][1].l};
+  }
+  return c;
+}
+
+// E1 - p*E2 per lane with only the high-word subtraction rounding (see
+// ff_sub_scaled_fast); np_h = -p.h.
+TCW_HD FF2 ff2_sub_scaled_fast(FF2 E1, F2 ph, F2 nph, F2 pl, FF2 E2) {
+  const F2 na = mul2(nph, E2.h);
+  F2 ae = fma2(ph, E2.h, na);
+  ae = fma2(ph, E2.l, ae);
+  ae = fma2(pl, E2.h, ae);
+  return FF2{add2(E1.h, na), sub2(E1.l, ae)};
+}
+
+// The same with an exact (TwoSum) high-word subtraction (tier 2).
+TCW_HD FF2 ff2_sub_scaled_exact(FF2 E1, F2 ph, F2 nph, F2 pl, FF2 E2) {
+  const F2 na = mul2(nph, E2.h);
+  F2 ae = fma2(ph, E2.h, na);
+  ae = fma2(ph, E2.l, ae);
+  ae = fma2(pl, E2.h, ae);
+  const F2 s = add2(E1.h, na);
+  const F2 bb = sub2(s, E1.h);
+  const F2 e = add2(sub2(E1.h, sub2(s, bb)), sub2(na, bb));
+  return FF2{s, sub2(add2(e, E1.l), ae)};
+}
+
+template <bool kFp64Det, class Sink>
+TCW_HD void exp_column2(const float *__restrict__ atoms8, const Geom &g,
+                        const uint32_t *__restrict__ t0s, uint32_t m_begin, uint32_t m_end,
+                        uint32_t tau, Sink &sink, const uint32_t *lo_tab = nullptr) {
+  const ExpConsts k = exp_consts(g.TAtom, tau);
+  const ExpConsts2 k2 = exp_consts2(k);
+  FF2 Elo[4], Ehi[4];
+  const F2 z{0.0f, 0.0f};
+#pragma unroll
+  for (int c = 0; c < 4; c++) Elo[c] = Ehi[c] = FF2{z, z};
+  uint32_t J = 0, jL = 0, jH = 0;
+  uint32_t nz = 0xFFFFFFFFu;  // first atom >= jL with a2 or b2 non-zero
+  uint32_t Lp = 0;            // exponent of the cached power pw = r1^Lp
+  FF pw{1.0f, 0.0f};
+  F2 ph[4], nph[4], pl[4];     // per-pair tail factors for the current Lp
+  bool pinit = false;
+  bool init = false;
+  for (uint32_t mm = m_end; mm > m_begin; mm--) {
+    const uint32_t m = mm - 1u;
+    const uint32_t t0 = t0s[m];
+    const uint32_t lo = lo_tab ? lo_tab[m - m_begin] : exp_lo(t0, g);
+    uint32_t hi;
+    if (!exp_hi(t0, tau, g, hi) || lo > hi) {
+      sink(m, 2.0f, false);
+      continue;
+    }
+    const uint32_t top = hi + 1u;
+    if (!init || top > J || lo > jL || top > jH) {
+      J = jL = jH = top;
+      nz = 0xFFFFFFFFu;
+#pragma unroll
+      for (int c = 0; c < 4; c++) Elo[c] = Ehi[c] = FF2{z, z};
+      init = true;
+    }
+    while (jH > top) {
+      jH--;
+      F2 x[4];
+      load_row8(atoms8 + (size_t)jH * 8u, x);
+#pragma unroll
+      for (int c = 0; c < 4; c++) Ehi[c] = ff2_axpy(x[c], k2.rh[c], k2.nrh[c], k2.rl[c], Ehi[c]);
+    }
+    while (jL > lo) {
+      jL--;
+      F2 x[4];
+      load_row8(atoms8 + (size_t)jL * 8u, x);
+#pragma unroll
+      for (int c = 0; c < 4; c++) Elo[c] = ff2_axpy(x[c], k2.rh[c], k2.nrh[c], k2.rl[c], Elo[c]);
+      if (x[0].x != 0.0f || x[0].y != 0.0f) nz = jL;
+    }
+    if (nz > hi) {  // no data in the window: zero sums, cond = inf
+      sink(m, 2.0f, false);
+      continue;
+    }
+    bool ok;
+    float F;
+    if (top == J) {
+      F = fstat_tiered2<kFp64Det>(Elo, ok);
+    } else {
+      const uint32_t L = top - lo;
+      if (L != Lp || !pinit) {
+        if (pinit && L == Lp + 1u)
+          pw = ff_mul(pw, k.r1);
+        else if (pinit && L + 1u == Lp && k.has_inv)
+          pw = ff_mul(pw, k.r1inv);
+        else
+          pw = ff_pow(k.r1, L);
+        Lp = L;
+        pinit = true;
+        const FF p2 = ff_mul(pw, pw);
+        ph[0] = F2{p2.h, p2.h};
+        pl[0] = F2{p2.l, p2.l};
+        ph[1] = F2{p2.h, pw.h};
+        pl[1] = F2{p2.l, pw.l};
+        ph[2] = F2{pw.h, pw.h};
+        pl[2] = F2{pw.l, pw.l};
+        ph[3] = F2{pw.h, pw.h};
+        pl[3] = F2{pw.l, pw.l};
+#pragma unroll
+        for (int c = 0; c < 4; c++) nph[c] = F2{-ph[c].x, -ph[c].y};
+      }
+      FF2 W[4];
+#pragma unroll
+      for (int c = 0; c < 4; c++) W[c] = ff2_sub_scaled_fast(Elo[c], ph[c], nph[c], pl[c], Ehi[c]);
+      const F2 s0 = add2(W[0].h, W[0].l), s1 = add2(W[1].h, W[1].l);
+      const F2 s2 = add2(W[2].h, W[2].l), s3 = add2(W[3].h, W[3].l);
+      if (fstat_fast_sums(s0.x, s0.y, s1.x, s1.y, s2.x, s2.y, s3.x, F)) {
+        ok = true;
+      } else {
+#pragma unroll
+        for (int c = 0; c < 4; c++)
+          W[c] = ff2_sub_scaled_exact(Elo[c], ph[c], nph[c], pl[c], Ehi[c]);
+        FF Ws[7];
+        ff2_unpack(W, Ws);
+        F = fstat_ff<kFp64Det>(Ws[0], Ws[1], Ws[2], Ws[3], Ws[4], Ws[5], Ws[6], ok);
       }
     }
     sink(m, F, ok);

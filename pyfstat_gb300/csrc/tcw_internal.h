@@ -25,6 +25,7 @@ struct TemplateDev {
   uint64_t t0_off;
   uint64_t tau_off;
   uint64_t p_off;
+  uint64_t a8_off;  // exp templates: first row in the 8-float atom rows
   uint64_t map_off;
   Geom g;
   uint32_t window;  // 1 rect, 2 exp
@@ -58,6 +59,9 @@ struct Partial {
 // Launchers (tcw_kernels.cu).  All asynchronous on `stream`.
 cudaError_t launch_prefix(const TemplateDev *d_T, const uint32_t *d_rect_list, uint32_t n_rect,
                           const float *d_atoms, float *d_P, int prec, cudaStream_t stream);
+// Exp templates' atoms (rows of 7 floats) into rows of 8 (zero-padded).
+cudaError_t launch_repack(const TemplateDev *d_T, const uint32_t *d_exp_list, uint32_t n_exp,
+                          const float *d_atoms, float *d_atoms8, cudaStream_t stream);
 struct MapLaunch {
   const TemplateDev *T;
   const WorkItem *items;  // this window's tiles
@@ -68,6 +72,7 @@ struct MapLaunch {
   int prec;
   int priority;           // stream-priority value of the launch
   const float *atoms;
+  const float *atoms8;    // exp tiles: atoms in 32-byte rows
   const uint32_t *t0s, *taus;
   const float *P;
   float *Fmn;

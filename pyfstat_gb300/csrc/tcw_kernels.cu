@@ -38,15 +38,31 @@ __device__ __forceinline__ FF shfl_up_ff(FF v, int d) {
   return FF{__shfl_up_sync(0xffffffffu, v.h, d), __shfl_up_sync(0xffffffffu, v.l, d)};
 }
 
+// One 64-byte prefix row as two 256-bit loads (each lane's request covers
+// whole 32-byte sectors).
 __device__ __forceinline__ void ld_row16(const float *p, float r[16]) {
-  const float4 *q = reinterpret_cast<const float4 *>(p);
 #pragma unroll
-  for (int k = 0; k < 4; k++) {
-    float4 v = __ldg(q + k);
-    r[4 * k + 0] = v.x;
-    r[4 * k + 1] = v.y;
-    r[4 * k + 2] = v.z;
-    r[4 * k + 3] = v.w;
+  for (int k = 0; k < 2; k++)
+    asm volatile("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=f"(r[8 * k + 0]), "=f"(r[8 * k + 1]), "=f"(r[8 * k + 2]),
+                   "=f"(r[8 * k + 3]), "=f"(r[8 * k + 4]), "=f"(r[8 * k + 5]),
+                   "=f"(r[8 * k + 6]), "=f"(r[8 * k + 7])
+                 : "l"(p + 8 * k));
+}
+
+// ------------------------------------------------------------------ repack
+
+__global__ void __launch_bounds__(256) repack_kernel(const TemplateDev *__restrict__ T,
+                                                     const uint32_t *__restrict__ exp_list,
+                                                     const float *__restrict__ atoms,
+                                                     float *__restrict__ A8) {
+  const TemplateDev t = T[exp_list[blockIdx.x]];
+  const float *x = atoms + t.atom_off * 7u;
+  float4 *o = reinterpret_cast<float4 *>(A8 + t.a8_off * 8u);
+  for (uint32_t i = threadIdx.x; i < t.g.numAtoms; i += blockDim.x) {
+    const float *r = x + (size_t)i * 7u;
+    o[2u * i] = make_float4(__ldg(r), __ldg(r + 1), __ldg(r + 2), __ldg(r + 3));
+    o[2u * i + 1u] = make_float4(__ldg(r + 4), __ldg(r + 5), __ldg(r + 6), 0.0f);
   }
 }
 
@@ -292,17 +308,22 @@ __device__ void rect_tile(const TemplateDev &t, const WorkItem &w,
       float F = 2.0f;
       if (row_ok) {
         if (e_cur >= j0) {
-          FF W[7];
-#pragma unroll
-          for (int c = 0; c < 7; c++) {
-            W[c].h = fsub(cur[c], row0[c]);
-            W[c].l = fsub(cur[8 + c], row0[8 + c]);
-          }
           bool ok;
-          if (kPrec == kPrecPlain32)
-            F = fstat_plain32(W[0].h, W[1].h, W[2].h, W[3].h, W[4].h, W[5].h, W[6].h, ok);
-          else
-            F = fstat_tiered<kPrec == kPrecFF_F64Det>(W, ok);
+          if (kPrec == kPrecPlain32) {
+            F = fstat_plain32(fsub(cur[0], row0[0]), fsub(cur[1], row0[1]),
+                              fsub(cur[2], row0[2]), fsub(cur[3], row0[3]),
+                              fsub(cur[4], row0[4]), fsub(cur[5], row0[5]),
+                              fsub(cur[6], row0[6]), ok);
+          } else {
+            FF2 W[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+              W[k].h = sub2(F2{cur[2 * k], cur[2 * k + 1]}, F2{row0[2 * k], row0[2 * k + 1]});
+              W[k].l = sub2(F2{cur[8 + 2 * k], cur[9 + 2 * k]},
+                            F2{row0[8 + 2 * k], row0[9 + 2 * k]});
+            }
+            F = fstat_tiered2<kPrec == kPrecFF_F64Det>(W, ok);
+          }
         }
         red.add(F, rowidx + n);
       }
@@ -342,6 +363,7 @@ constexpr uint32_t kExpLoTab = 2048;
 
 template <bool kWrite, int kPrec>
 __device__ void exp_tile(const TemplateDev &t, const WorkItem &w, const float *__restrict__ atoms,
+                         const float *__restrict__ atoms8,
                          const uint32_t *__restrict__ t0s_all,
                          const uint32_t *__restrict__ taus_all, float *__restrict__ Fmn,
                          Red &red, uint32_t *lo_tab) {
@@ -362,14 +384,13 @@ __device__ void exp_tile(const TemplateDev &t, const WorkItem &w, const float *_
     const uint32_t me = min(w.m1, mb + R);
     const uint32_t tau = __ldg(taus_all + t.tau_off + n);
     MapSink<kWrite> sink{kWrite ? Fmn + t.map_off : nullptr, t.N_tau, n, &red};
-    const float *x = atoms + t.atom_off * 7u;
     const uint32_t *tab = use_tab ? lo_tab + (mb - w.m0) : nullptr;
     if (kPrec == kPrecPlain32)
-      exp_column<false, false>(x, t.g, t0s, mb, me, tau, sink, tab);
+      exp_column<false, false>(atoms + t.atom_off * 7u, t.g, t0s, mb, me, tau, sink, tab);
     else if (kPrec == kPrecFF_F64Det)
-      exp_column<true, true>(x, t.g, t0s, mb, me, tau, sink, tab);
+      exp_column2<true>(atoms8 + t.a8_off * 8u, t.g, t0s, mb, me, tau, sink, tab);
     else
-      exp_column<true, false>(x, t.g, t0s, mb, me, tau, sink, tab);
+      exp_column2<false>(atoms8 + t.a8_off * 8u, t.g, t0s, mb, me, tau, sink, tab);
   }
 }
 
@@ -377,7 +398,8 @@ template <int kWin, bool kPersist, bool kWrite, int kPrec>
 __global__ void __launch_bounds__(kBlock)
     map_kernel(const TemplateDev *__restrict__ T, const WorkItem *__restrict__ items,
                uint32_t n_items, uint32_t *__restrict__ counter, const float *__restrict__ atoms,
-               const uint32_t *__restrict__ t0s, const uint32_t *__restrict__ taus,
+               const float *__restrict__ atoms8, const uint32_t *__restrict__ t0s,
+               const uint32_t *__restrict__ taus,
                const float *__restrict__ P, float *__restrict__ Fmn,
                Partial *__restrict__ parts) {
   __shared__ uint32_t s_item;
@@ -401,7 +423,7 @@ __global__ void __launch_bounds__(kBlock)
       rect_tile<kWrite, kPrec>(t, w, t0s, taus, P, Fmn, red,
                                reinterpret_cast<float *>(sm) + (threadIdx.x >> 5) * (32 * 33));
     else
-      exp_tile<kWrite, kPrec>(t, w, atoms, t0s, taus, Fmn, red, sm);
+      exp_tile<kWrite, kPrec>(t, w, atoms, atoms8, t0s, taus, Fmn, red, sm);
     block_reduce_store(red, parts + w.part);
     if (!kPersist) break;
   }
@@ -574,9 +596,9 @@ cudaError_t launch_prefix(const TemplateDev *d_T, const uint32_t *d_rect_list, u
 template <int kWin, bool kPersist, bool kWrite>
 static cudaError_t launch_map_prec(int prec, uint32_t grid, cudaStream_t s, int priority,
                                    const TemplateDev *T, const WorkItem *items, uint32_t n_items,
-                                   uint32_t *counter, const float *atoms, const uint32_t *t0s,
-                                   const uint32_t *taus, const float *P, float *Fmn,
-                                   Partial *parts) {
+                                   uint32_t *counter, const float *atoms, const float *atoms8,
+                                   const uint32_t *t0s, const uint32_t *taus, const float *P,
+                                   float *Fmn, Partial *parts) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(kBlock);
@@ -588,12 +610,12 @@ static cudaError_t launch_map_prec(int prec, uint32_t grid, cudaStream_t s, int 
   cfg.numAttrs = 1;
   if (prec == kPrecPlain32)
     return cudaLaunchKernelEx(&cfg, map_kernel<kWin, kPersist, kWrite, kPrecPlain32>, T, items,
-                              n_items, counter, atoms, t0s, taus, P, Fmn, parts);
+                              n_items, counter, atoms, atoms8, t0s, taus, P, Fmn, parts);
   if (prec == kPrecFF_F64Det)
     return cudaLaunchKernelEx(&cfg, map_kernel<kWin, kPersist, kWrite, kPrecFF_F64Det>, T, items,
-                              n_items, counter, atoms, t0s, taus, P, Fmn, parts);
+                              n_items, counter, atoms, atoms8, t0s, taus, P, Fmn, parts);
   return cudaLaunchKernelEx(&cfg, map_kernel<kWin, kPersist, kWrite, kPrecFF>, T, items, n_items,
-                            counter, atoms, t0s, taus, P, Fmn, parts);
+                            counter, atoms, atoms8, t0s, taus, P, Fmn, parts);
 }
 
 template <int kWin>
@@ -603,19 +625,26 @@ static cudaError_t launch_map_win(const MapLaunch &L, cudaStream_t stream) {
   if (L.persistent) {
     if (L.write_map)
       return launch_map_prec<kWin, true, true>(L.prec, grid, stream, L.priority, L.T, L.items,
-                                               L.n_items, L.counter, L.atoms, L.t0s, L.taus, L.P,
+                                               L.n_items, L.counter, L.atoms, L.atoms8, L.t0s, L.taus, L.P,
                                                L.Fmn, L.parts);
     return launch_map_prec<kWin, true, false>(L.prec, grid, stream, L.priority, L.T, L.items,
-                                              L.n_items, L.counter, L.atoms, L.t0s, L.taus, L.P,
+                                              L.n_items, L.counter, L.atoms, L.atoms8, L.t0s, L.taus, L.P,
                                               L.Fmn, L.parts);
   }
   if (L.write_map)
     return launch_map_prec<kWin, false, true>(L.prec, grid, stream, L.priority, L.T, L.items,
-                                              L.n_items, L.counter, L.atoms, L.t0s, L.taus, L.P,
+                                              L.n_items, L.counter, L.atoms, L.atoms8, L.t0s, L.taus, L.P,
                                               L.Fmn, L.parts);
   return launch_map_prec<kWin, false, false>(L.prec, grid, stream, L.priority, L.T, L.items,
-                                             L.n_items, L.counter, L.atoms, L.t0s, L.taus, L.P,
+                                             L.n_items, L.counter, L.atoms, L.atoms8, L.t0s, L.taus, L.P,
                                              L.Fmn, L.parts);
+}
+
+cudaError_t launch_repack(const TemplateDev *d_T, const uint32_t *d_exp_list, uint32_t n_exp,
+                          const float *d_atoms, float *d_atoms8, cudaStream_t stream) {
+  if (n_exp == 0) return cudaSuccess;
+  repack_kernel<<<n_exp, 256, 0, stream>>>(d_T, d_exp_list, d_atoms, d_atoms8);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_map(int window, const MapLaunch &L, cudaStream_t stream) {

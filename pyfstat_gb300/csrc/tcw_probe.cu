@@ -40,6 +40,30 @@ __global__ void __launch_bounds__(256) probe_fp64(double *out, double a, double 
   if (s == 1234.5) out[0] = s;
 }
 
+__global__ void __launch_bounds__(256) probe_fp32x2(float *out, float a, float b) {
+  unsigned long long v[kChains], A, B;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(A) : "f"(a), "f"(a));
+  asm("mov.b64 %0, {%1, %2};" : "=l"(B) : "f"(b), "f"(b));
+#pragma unroll
+  for (int c = 0; c < kChains; c++) {
+    float x = threadIdx.x * 1e-3f + c;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(v[c]) : "f"(x), "f"(x + 0.5f));
+  }
+  for (int i = 0; i < kIters; i++) {
+#pragma unroll
+    for (int c = 0; c < kChains; c++)
+      asm volatile("fma.rn.f32x2 %0, %0, %1, %2;" : "+l"(v[c]) : "l"(A), "l"(B));
+  }
+  float s = 0.0f;
+#pragma unroll
+  for (int c = 0; c < kChains; c++) {
+    float x, y;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(v[c]));
+    s += x + y;
+  }
+  if (s == 1234.5f) out[0] = s;
+}
+
 __device__ __forceinline__ float ex2_approx(float x) {
   float y;
   asm volatile("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
@@ -82,9 +106,11 @@ float time_ms(F launch, cudaStream_t s, int reps) {
 extern "C" {
 
 // Measured peaks of `device`: FP32 and FP64 in TFLOP/s (an FMA counts 2),
-// MUFU ex2 in tera-operations/s.  Measurement utility with no counterpart in
+// MUFU ex2 in tera-operations/s, and FP32 through packed fma.rn.f32x2
+// (4 flops per instruction).  Measurement utility with no counterpart in
 // the reference; takes well under a second.
-int tcw_probe_peaks(int device, double *fp32_tflops, double *fp64_tflops, double *mufu_tops) {
+int tcw_probe_peaks(int device, double *fp32_tflops, double *fp64_tflops, double *mufu_tops,
+                    double *fp32x2_tflops) {
   if (cudaSetDevice(device) != cudaSuccess) {
     cudaGetLastError();
     return TCW_ERR_NO_DEVICE;
@@ -105,6 +131,7 @@ int tcw_probe_peaks(int device, double *fp32_tflops, double *fp64_tflops, double
     probe_fp64<<<blocks, threads, 0, s>>>(reinterpret_cast<double *>(buf), 0.999, 1e-3);
   }, s, 3);
   float msmu = time_ms([&] { probe_mufu<<<blocks, threads, 0, s>>>(buf, 0.5f); }, s, 5);
+  float ms2 = time_ms([&] { probe_fp32x2<<<blocks, threads, 0, s>>>(buf, 0.999f, 1e-3f); }, s, 5);
   cudaError_t e = cudaGetLastError();
   cudaStreamDestroy(s);
   cudaFree(buf);
@@ -112,6 +139,7 @@ int tcw_probe_peaks(int device, double *fp32_tflops, double *fp64_tflops, double
   if (fp32_tflops) *fp32_tflops = 2.0 * nthr * kChains * kIters / (ms32 * 1e-3) / 1e12;
   if (fp64_tflops) *fp64_tflops = 2.0 * nthr * kChains * (kIters / 16) / (ms64 * 1e-3) / 1e12;
   if (mufu_tops) *mufu_tops = nthr * kChains * (kIters / 4) / (msmu * 1e-3) / 1e12;
+  if (fp32x2_tflops) *fp32x2_tflops = 4.0 * nthr * kChains * kIters / (ms2 * 1e-3) / 1e12;
   return TCW_OK;
 }
 

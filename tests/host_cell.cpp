@@ -83,21 +83,28 @@ struct HostSink {
   }
 };
 
+// comp = 1: the packed column the GPU runs (atoms in rows of 8);
+// comp = 0: the uncompensated FP32 variant.
 int hc_exp_map(const float *atoms, uint32_t n, uint32_t TAtom, uint32_t t0_data,
                const uint32_t *t0s, uint32_t N_t0, const uint32_t *taus, uint32_t N_tau,
                int comp, uint32_t row_chunk, float *F, uint8_t *okmap) {
   Geom g = make_geom(n, TAtom, t0_data);
   if (row_chunk == 0) row_chunk = N_t0;
+  float *a8 = (float *)calloc((size_t)n * 8u, sizeof(float));
+  if (!a8) return -1;
+  for (uint32_t i = 0; i < n; i++)
+    for (int c = 0; c < 7; c++) a8[(size_t)i * 8u + c] = atoms[(size_t)i * 7u + c];
   for (uint32_t k = 0; k < N_tau; k++) {
     for (uint32_t mb = 0; mb < N_t0; mb += row_chunk) {
       uint32_t me = mb + row_chunk < N_t0 ? mb + row_chunk : N_t0;
       HostSink s{F + k, okmap ? okmap + k : nullptr, N_tau};
       if (comp)
-        exp_column<true, false>(atoms, g, t0s, mb, me, taus[k], s);
+        exp_column2<false>(a8, g, t0s, mb, me, taus[k], s);
       else
         exp_column<false, false>(atoms, g, t0s, mb, me, taus[k], s);
     }
   }
+  free(a8);
   return 0;
 }
 
