@@ -157,6 +157,27 @@ int tcw_plan_run_timed(tcw_handle *h, tcw_plan *plan, const float *d_atoms, tcw_
 int tcw_probe_peaks(int device, double *fp32_tflops, double *fp64_tflops, double *mufu_tops,
                     double *fp32x2_tflops);
 
+/* Scratch size of tcw_map_plain_noalloc (bytes). */
+#define TCW_NOALLOC_SCRATCH_BYTES (16u << 20)
+
+/* The plain per-template map for callers that may not allocate device
+ * memory (no cudaMalloc / cudaFree and no allocating library routine is
+ * called).  It has no counterpart in the reference.  Same arguments, results
+ * and flags as tcw_map_plain, with a stream (cudaStream_t, NULL for the
+ * legacy default stream) instead of a handle; runs on the current device.
+ * Its scratch is one static device array of TCW_NOALLOC_SCRATCH_BYTES that
+ * every GPU loading this library holds until the process exits.  A problem
+ * needing more -- 256-byte-aligned sections of 64 B x (numAtoms+1) prefix
+ * rows (rect) or 32 B x numAtoms atom rows (exp), 56 B per tile, and with
+ * TCW_FLAG_POSTERIORS 8 B x (N_t0 + ceil(N_t0/64) x N_tau) -- is rejected
+ * with TCW_ERR_OVERFLOW.  The first call on a device looks the array's
+ * address up: make it before any stream capture.  Calls share the array:
+ * calls whose work overlaps on the GPU race and must be serialised. */
+int tcw_map_plain_noalloc(void *stream, const float *d_atoms, uint32_t numAtoms, uint32_t TAtom,
+                          uint32_t t0_data, int window, const uint32_t *d_t0s, uint32_t N_t0,
+                          const uint32_t *d_taus, uint32_t N_tau, float *d_Fmn,
+                          tcw_result *d_result, int flags);
+
 /* Test hook: make the n-th following workspace allocation on this handle
  * fail (n = 0 disables).  Host-side only; used to test error paths. */
 int tcw_debug_fail_alloc(tcw_handle *h, int n);

@@ -92,6 +92,8 @@ SIGNATURES = {
     "tcw_plan_run_host": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
     "tcw_plan_run_timed": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.POINTER(ctypes.c_float)]),
     "tcw_debug_fail_alloc": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "tcw_map_plain_noalloc": (ctypes.c_int, [_vp, _vp, _c_u32, _c_u32, _c_u32, ctypes.c_int, _vp,
+                                             _c_u32, _vp, _c_u32, _vp, _vp, ctypes.c_int]),
     "tcw_probe_peaks": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                        ctypes.POINTER(ctypes.c_double),
                                        ctypes.POINTER(ctypes.c_double),
@@ -253,6 +255,27 @@ class Handle:
                                   int(t0_data), int(window), _p(d_t0s), int(N_t0), _p(d_taus),
                                   int(N_tau), _p(d_Fmn), _p(d_result), int(flags))
         check(rc, self.ptr)
+
+
+NOALLOC_SCRATCH_BYTES = 16 << 20
+
+
+def map_plain_noalloc(stream, d_atoms, numAtoms, TAtom, t0_data, window, d_t0s, N_t0, d_taus,
+                      N_tau, d_Fmn, d_result, flags=TCW_FLAG_LNBTSG):
+    """The plain map without any device allocation, for callers that may not
+    allocate: its scratch is a fixed static device array
+    (NOALLOC_SCRATCH_BYTES); larger problems raise TcwError(TCW_ERR_OVERFLOW).
+    Runs asynchronously on ``stream`` (a raw cudaStream_t pointer) on the
+    current device.  Calls whose work overlaps on the GPU share the scratch
+    and must be serialised."""
+    rc = load().tcw_map_plain_noalloc(stream, _p(d_atoms), int(numAtoms), int(TAtom),
+                                      int(t0_data), int(window), _p(d_t0s), int(N_t0),
+                                      _p(d_taus), int(N_tau), _p(d_Fmn), _p(d_result),
+                                      int(flags))
+    if rc == TCW_ERR_OVERFLOW:
+        raise TcwError(rc, "problem needs more scratch than the no-allocation entry point's "
+                           f"{NOALLOC_SCRATCH_BYTES} bytes (or times exceed the u32 range)")
+    check(rc)
 
 
 def _p(x):
