@@ -394,8 +394,18 @@ __device__ void exp_tile(const TemplateDev &t, const WorkItem &w, const float *_
   }
 }
 
+// Minimum resident blocks per SM requested from the register allocator
+// (build-time tunables; 1 leaves the allocation to ptxas).
+#ifndef TCW_RECT_MIN_BLOCKS
+#define TCW_RECT_MIN_BLOCKS 1
+#endif
+#ifndef TCW_EXP_MIN_BLOCKS
+#define TCW_EXP_MIN_BLOCKS 5
+#endif
+
 template <int kWin, bool kPersist, bool kWrite, int kPrec>
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kBlock, kWin == TCW_WINDOW_RECT ? TCW_RECT_MIN_BLOCKS
+                                                                  : TCW_EXP_MIN_BLOCKS)
     map_kernel(const TemplateDev *__restrict__ T, const WorkItem *__restrict__ items,
                uint32_t n_items, uint32_t *__restrict__ counter, const float *__restrict__ atoms,
                const float *__restrict__ atoms8, const uint32_t *__restrict__ t0s,
