@@ -150,6 +150,39 @@ int tcw_plan_run_host(tcw_handle *h, tcw_plan *plan, const float *atoms, tcw_res
 int tcw_plan_run_timed(tcw_handle *h, tcw_plan *plan, const float *d_atoms, tcw_result *d_results,
                        float *ms);
 
+/* Differentiable exponential-window maps (no counterpart in the reference:
+ * an addition for gradient-based searches).  Per template the tau grid is
+ * continuous, tau_n = tau_min + n (tau_max - tau_min) / (N_tau - 1); the
+ * t0 grid (host array, seconds) must be non-decreasing and start no earlier
+ * than t0_data - TAtom/2.  Outputs per template: lnBtSG (ln(70/(N_t0 N_tau))
+ * + logsumexp F) and softmax2F = T logsumexp(2F/T).  F is evaluated in FP64
+ * here (gradients of the T = 0.1 soft-max need F to ~1e-9). */
+typedef struct {
+  uint64_t atom_offset; /* first row of this template in the concatenated atoms */
+  uint64_t t0_offset;   /* first entry in the concatenated t0 grid */
+  uint32_t numAtoms;
+  uint32_t TAtom;
+  uint32_t t0_data;
+  uint32_t N_t0;
+  uint32_t N_tau;
+  uint32_t pad;
+  double tau_min;
+  double tau_max;
+} tcw_diff_desc;
+
+int tcw_expdiff_forward(tcw_handle *h, const tcw_diff_desc *desc, uint32_t n_templates,
+                        const float *d_atoms, const uint32_t *t0s, uint64_t n_t0s,
+                        double temperature, double *d_lnBtSG, double *d_softmax2F);
+/* Gradients of L(lnBtSG, softmax2F) given dL/dlnBtSG and dL/dsoftmax2F per
+ * template (device arrays) and the forward's outputs: d_grad_atoms
+ * (n_atom_rows x 7, FP64, overwritten) and d_grad_tau (n_templates x 2:
+ * dL/dtau_min, dL/dtau_max, overwritten).  Recomputes the window sums. */
+int tcw_expdiff_backward(tcw_handle *h, const tcw_diff_desc *desc, uint32_t n_templates,
+                         const float *d_atoms, const uint32_t *t0s, uint64_t n_t0s,
+                         double temperature, const double *d_lnBtSG, const double *d_softmax2F,
+                         const double *d_grad_lnBtSG, const double *d_grad_softmax2F,
+                         double *d_grad_atoms, uint64_t n_atom_rows, double *d_grad_tau);
+
 /* Measured throughput of `device` for roofline denominators: FP32 and FP64
  * FMA in TFLOP/s (an FMA counts 2), MUFU ex2 in Tops/s, FP32 through packed
  * f32x2 FMAs in TFLOP/s.  A measurement utility; it has no counterpart in the

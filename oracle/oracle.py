@@ -72,6 +72,10 @@ def _load():
                                            ctypes.c_uint32, ctypes.c_int, _u32p, _u32p,
                                            ctypes.c_uint64, _f64p]
         lib.tcwo_cell_sums_f64.restype = ctypes.c_int
+        lib.tcwo_exp_map_f64_realtau.argtypes = [_f32p, ctypes.c_uint32, ctypes.c_uint32,
+                                                 ctypes.c_uint32, _u32p, ctypes.c_uint32, _f64p,
+                                                 ctypes.c_uint32, _f64p, ctypes.c_int]
+        lib.tcwo_exp_map_f64_realtau.restype = ctypes.c_int
         for name in ("tcwo_idx_start", "tcwo_idx_end"):
             fn = getattr(lib, name)
             fn.argtypes = [ctypes.c_uint32] * 4
@@ -164,6 +168,22 @@ def cell_sums_f64(atoms7, TAtom, t0_data, window, t0s, taus):
     if rc != 0:
         raise ValueError(f"oracle cell_sums_f64 failed with status {rc}")
     return out
+
+
+def exp_map_f64_realtau(atoms7, TAtom, t0_data, t0s, taus, nthreads=0):
+    """FP64 exponential-window map on a real-valued tau grid (differentiable variant)."""
+    lib = _load()
+    a = _atoms(atoms7)
+    t0s = _c(t0s, np.uint32)
+    taus = _c(taus, np.float64)
+    F = np.empty((len(t0s), len(taus)), dtype=np.float64)
+    rc = lib.tcwo_exp_map_f64_realtau(a.ctypes.data_as(_f32p), a.shape[0], int(TAtom),
+                                      int(t0_data), t0s.ctypes.data_as(_u32p), len(t0s),
+                                      taus.ctypes.data_as(_f64p), len(taus),
+                                      F.ctypes.data_as(_f64p), int(nthreads))
+    if rc != 0:
+        raise ValueError(f"oracle exp_map_f64_realtau failed with status {rc}")
+    return F
 
 
 def idx_start(t0, t0_data, TAtom, numAtoms):

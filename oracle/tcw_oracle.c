@@ -331,6 +331,46 @@ int tcwo_cell_sums_f64(const float *atoms, uint32_t numAtoms, uint32_t TAtom,
   return 0;
 }
 
+/* Exponential window with a real-valued tau (the differentiable variant):
+ * t1 = t0 + 3 tau in FP64; the end index is the reference's formula with t1
+ * real, i_t1 = clamp(floor((t1 - t0_data + TAtom/2) / TAtom) - 1), and atoms
+ * count while t0 <= t_i <= t1.  For integral tau (no u32 wrap) this is the
+ * reference's window.  Returns F in FP64. */
+static double cell_f64_realtau(const float *atoms, uint32_t numAtoms, uint32_t TAtom,
+                               uint32_t t0_data, uint32_t t0, double tau, double *cond) {
+  uint32_t i_t0 = idx_start(t0, t0_data, TAtom, numAtoms);
+  double t1 = (double)t0 + 3.0 * tau;
+  double s[7] = {0, 0, 0, 0, 0, 0, 0};
+  if (t1 >= (double)t0_data) {
+    double q = floor((t1 - (double)t0_data + (double)(TAtom / 2u)) / (double)TAtom) - 1.0;
+    uint32_t i_t1 = q < 0.0 ? 0u : (q >= (double)(numAtoms - 1u) ? numAtoms - 1u : (uint32_t)q);
+    for (uint32_t i = i_t0; i <= i_t1; i++) {
+      double t_i = (double)t0_data + (double)i * (double)TAtom;
+      if (!(t_i >= (double)t0 && t_i <= t1)) continue;
+      double w = exp(-(t_i - (double)t0) / tau);
+      double w2 = w * w;
+      const float *x = atoms + (size_t)i * 7u;
+      for (int c = 0; c < 3; c++) s[c] += (double)x[c] * w2;
+      for (int c = 3; c < 7; c++) s[c] += (double)x[c] * w;
+    }
+  }
+  return fstat_f64(s[0], s[1], s[2], s[3], s[4], s[5], s[6], cond);
+}
+
+int tcwo_exp_map_f64_realtau(const float *atoms, uint32_t numAtoms, uint32_t TAtom,
+                             uint32_t t0_data, const uint32_t *t0s, uint32_t N_t0,
+                             const double *taus, uint32_t N_tau, double *Fmn, int nthreads) {
+  if (!atoms || !t0s || !taus || !Fmn) return -1;
+  if (numAtoms == 0 || TAtom == 0 || N_t0 == 0 || N_tau == 0) return -2;
+  set_threads(nthreads);
+#pragma omp parallel for collapse(2) schedule(dynamic, 16)
+  for (int64_t m = 0; m < (int64_t)N_t0; m++)
+    for (int64_t n = 0; n < (int64_t)N_tau; n++)
+      Fmn[(size_t)m * N_tau + n] =
+          cell_f64_realtau(atoms, numAtoms, TAtom, t0_data, t0s[m], taus[n], NULL);
+  return 0;
+}
+
 /* Index helpers exported so tests can pin the u32 wrap-around semantics. */
 uint32_t tcwo_idx_start(uint32_t t0, uint32_t t0_data, uint32_t TAtom,
                         uint32_t numAtoms) {

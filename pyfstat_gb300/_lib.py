@@ -61,6 +61,11 @@ RESULT_DTYPE = np.dtype([("lnBtSG", "<f8"), ("argmax", "<i8"), ("t0_mp_idx", "<i
 DESC_DTYPE = np.dtype([("atom_offset", "<u8"), ("t0_offset", "<u8"), ("tau_offset", "<u8"),
                        ("numAtoms", "<u4"), ("TAtom", "<u4"), ("t0_data", "<u4"),
                        ("window", "<i4"), ("N_t0", "<u4"), ("N_tau", "<u4")])
+DIFF_DESC_DTYPE = np.dtype([("atom_offset", "<u8"), ("t0_offset", "<u8"), ("numAtoms", "<u4"),
+                            ("TAtom", "<u4"), ("t0_data", "<u4"), ("N_t0", "<u4"),
+                            ("N_tau", "<u4"), ("pad", "<u4"), ("tau_min", "<f8"),
+                            ("tau_max", "<f8")])
+assert DIFF_DESC_DTYPE.itemsize == 56
 assert RESULT_DTYPE.itemsize == ctypes.sizeof(TcwResult) == 40
 assert DESC_DTYPE.itemsize == ctypes.sizeof(TcwTemplateDesc) == 48
 
@@ -94,6 +99,10 @@ SIGNATURES = {
     "tcw_debug_fail_alloc": (ctypes.c_int, [_vp, ctypes.c_int]),
     "tcw_map_plain_noalloc": (ctypes.c_int, [_vp, _vp, _c_u32, _c_u32, _c_u32, ctypes.c_int, _vp,
                                              _c_u32, _vp, _c_u32, _vp, _vp, ctypes.c_int]),
+    "tcw_expdiff_forward": (ctypes.c_int, [_vp, _vp, _c_u32, _vp, _vp, _c_u64, ctypes.c_double,
+                                           _vp, _vp]),
+    "tcw_expdiff_backward": (ctypes.c_int, [_vp, _vp, _c_u32, _vp, _vp, _c_u64, ctypes.c_double,
+                                            _vp, _vp, _vp, _vp, _vp, _c_u64, _vp]),
     "tcw_probe_peaks": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                        ctypes.POINTER(ctypes.c_double),
                                        ctypes.POINTER(ctypes.c_double),

@@ -934,6 +934,150 @@ int tcw_plan_run_timed(tcw_handle *h, tcw_plan *p, const float *d_atoms, tcw_res
   return TCW_OK;
 }
 
+// ---------------------------------------------------------------- differentiable path
+
+// Validates descriptors, uploads descriptors, tiles and grids into the
+// handle's workspace; returns the layout of what follows them.
+struct DiffSetup {
+  size_t o_T, o_items, o_parts, o_t0, o_cnt, o_scratch, total;
+  uint32_t n_items, n_blocks, max_rows;
+};
+
+static int diff_prepare(tcw_handle *h, const tcw_diff_desc *desc, uint32_t n,
+                        const uint32_t *t0s, uint64_t n_t0s, int pass, DiffSetup &S) {
+  if (!desc || n == 0 || !t0s) return set_err(h, TCW_ERR_INVALID_ARG, "empty template list");
+  std::vector<DiffTemplate> T(n);
+  std::vector<DiffItem> items;
+  uint32_t max_rows = 0;
+  try {
+    for (uint32_t k = 0; k < n; k++) {
+      const tcw_diff_desc &d = desc[k];
+      int rc = check_geometry(h, d.numAtoms, d.TAtom, d.t0_data, d.N_t0, d.N_tau);
+      if (rc) return rc;
+      if (d.t0_offset + d.N_t0 > n_t0s)
+        return set_err(h, TCW_ERR_INVALID_ARG, "template %u: t0 grid outside the array", k);
+      if (!(d.tau_min > 0.0) || !(d.tau_max >= d.tau_min))
+        return set_err(h, TCW_ERR_INVALID_ARG, "template %u: need 0 < tau_min <= tau_max", k);
+      const uint32_t *g = t0s + d.t0_offset;
+      if ((uint64_t)g[0] + d.TAtom / 2u < d.t0_data)
+        return set_err(h, TCW_ERR_INVALID_ARG, "template %u: t0 grid starts before the data", k);
+      for (uint32_t m = 1; m < d.N_t0; m++)
+        if (g[m] < g[m - 1])
+          return set_err(h, TCW_ERR_INVALID_ARG, "template %u: t0 grid must be non-decreasing", k);
+      if ((double)g[d.N_t0 - 1] + 3.0 * d.tau_max >= 4294967295.0)
+        return set_err(h, TCW_ERR_OVERFLOW, "template %u: t0 + 3 tau exceeds the u32 range", k);
+      DiffTemplate t{};
+      t.atom_off = d.atom_offset;
+      t.t0_off = d.t0_offset;
+      t.g = make_geom(d.numAtoms, d.TAtom, d.t0_data);
+      t.N_t0 = d.N_t0;
+      t.N_tau = d.N_tau;
+      t.tau_min = d.tau_min;
+      t.tau_max = d.tau_max;
+      t.part_off = (uint32_t)items.size();
+      for (uint32_t n0 = 0; n0 < d.N_tau; n0 += 128u)
+        items.push_back(DiffItem{k, (uint32_t)items.size(), n0, std::min(d.N_tau, n0 + 128u)});
+      t.n_parts = (uint32_t)items.size() - t.part_off;
+      T[k] = t;
+      max_rows = std::max(max_rows, d.N_t0);
+    }
+  } catch (const std::bad_alloc &) {
+    return set_err(h, TCW_ERR_ALLOC, "host allocation failed");
+  }
+  S.n_items = (uint32_t)items.size();
+  S.max_rows = max_rows;
+  S.n_blocks = (uint32_t)std::max<uint64_t>(
+      1, std::min<uint64_t>(S.n_items, (uint64_t)diff_blocks_per_sm(pass) * h->n_sms));
+  Layout L;
+  S.o_T = L.add(sizeof(DiffTemplate) * n);
+  S.o_items = L.add(sizeof(DiffItem) * S.n_items);
+  S.o_t0 = L.add(sizeof(uint32_t) * n_t0s);
+  S.o_cnt = L.add(sizeof(uint32_t));
+  const size_t ctl = L.total;
+  S.o_parts = L.add(sizeof(DiffPartial) * S.n_items);
+  S.o_scratch = pass == 1 ? L.add(sizeof(float) * 8u * 128u * (size_t)max_rows * S.n_blocks) : 0;
+  S.total = L.total;
+  int rc = ensure_ws(h, S.total);
+  if (rc) return rc;
+  rc = ensure_stage(h, ctl);
+  if (rc) return rc;
+  memcpy(h->h_stage + S.o_T, T.data(), sizeof(DiffTemplate) * n);
+  memcpy(h->h_stage + S.o_items, items.data(), sizeof(DiffItem) * S.n_items);
+  memcpy(h->h_stage + S.o_t0, t0s, sizeof(uint32_t) * n_t0s);
+  memset(h->h_stage + S.o_cnt, 0, sizeof(uint32_t));
+  TCW_CUDA(h, cudaMemcpyAsync(h->d_ws, h->h_stage, ctl, cudaMemcpyHostToDevice, h->stream));
+  TCW_CUDA(h, cudaEventRecord(h->stage_ev, h->stream));
+  h->stage_pending = true;
+  return TCW_OK;
+}
+
+static DiffLaunch diff_launch(tcw_handle *h, const DiffSetup &S, const float *d_atoms,
+                              double temperature) {
+  DiffLaunch L{};
+  L.T = reinterpret_cast<const DiffTemplate *>(h->d_ws + S.o_T);
+  L.items = reinterpret_cast<const DiffItem *>(h->d_ws + S.o_items);
+  L.n_items = S.n_items;
+  L.n_blocks = S.n_blocks;
+  L.counter = reinterpret_cast<uint32_t *>(h->d_ws + S.o_cnt);
+  L.atoms = d_atoms;
+  L.t0s = reinterpret_cast<const uint32_t *>(h->d_ws + S.o_t0);
+  L.temp = temperature;
+  L.parts = reinterpret_cast<DiffPartial *>(h->d_ws + S.o_parts);
+  return L;
+}
+
+int tcw_expdiff_forward(tcw_handle *h, const tcw_diff_desc *desc, uint32_t n_templates,
+                        const float *d_atoms, const uint32_t *t0s, uint64_t n_t0s,
+                        double temperature, double *d_lnBtSG, double *d_softmax2F) {
+  if (!h) return TCW_ERR_INVALID_ARG;
+  if (!d_atoms || !d_lnBtSG || !d_softmax2F)
+    return set_err(h, TCW_ERR_INVALID_ARG, "null device pointer");
+  if (!(temperature > 0.0)) return set_err(h, TCW_ERR_INVALID_ARG, "temperature must be > 0");
+  int rc = set_device(h);
+  if (rc) return rc;
+  DiffSetup S;
+  rc = diff_prepare(h, desc, n_templates, t0s, n_t0s, 0, S);
+  if (rc) return rc;
+  DiffLaunch L = diff_launch(h, S, d_atoms, temperature);
+  TCW_CUDA(h, launch_diff(0, L, h->stream));
+  TCW_CUDA(h, launch_diff_finalize(L.T, n_templates, L.parts, temperature, d_lnBtSG, d_softmax2F,
+                                   h->stream));
+  return TCW_OK;
+}
+
+int tcw_expdiff_backward(tcw_handle *h, const tcw_diff_desc *desc, uint32_t n_templates,
+                         const float *d_atoms, const uint32_t *t0s, uint64_t n_t0s,
+                         double temperature, const double *d_lnBtSG, const double *d_softmax2F,
+                         const double *d_grad_lnBtSG, const double *d_grad_softmax2F,
+                         double *d_grad_atoms, uint64_t n_atom_rows, double *d_grad_tau) {
+  if (!h) return TCW_ERR_INVALID_ARG;
+  if (!d_atoms || !d_lnBtSG || !d_softmax2F || !d_grad_lnBtSG || !d_grad_softmax2F ||
+      !d_grad_atoms || !d_grad_tau)
+    return set_err(h, TCW_ERR_INVALID_ARG, "null device pointer");
+  if (!(temperature > 0.0)) return set_err(h, TCW_ERR_INVALID_ARG, "temperature must be > 0");
+  for (uint32_t k = 0; desc && k < n_templates; k++)
+    if (desc[k].atom_offset + desc[k].numAtoms > n_atom_rows)
+      return set_err(h, TCW_ERR_INVALID_ARG, "template %u: atoms outside the gradient array", k);
+  int rc = set_device(h);
+  if (rc) return rc;
+  DiffSetup S;
+  rc = diff_prepare(h, desc, n_templates, t0s, n_t0s, 1, S);
+  if (rc) return rc;
+  DiffLaunch L = diff_launch(h, S, d_atoms, temperature);
+  L.lnZ1 = d_lnBtSG;
+  L.lnZ2 = d_softmax2F;
+  L.gB = d_grad_lnBtSG;
+  L.gS = d_grad_softmax2F;
+  L.scratch = reinterpret_cast<float *>(h->d_ws + S.o_scratch);
+  L.scratch_rows = S.max_rows;
+  L.grad_atoms = d_grad_atoms;
+  L.grad_tau = d_grad_tau;
+  TCW_CUDA(h, cudaMemsetAsync(d_grad_atoms, 0, sizeof(double) * 7u * n_atom_rows, h->stream));
+  TCW_CUDA(h, cudaMemsetAsync(d_grad_tau, 0, sizeof(double) * 2u * n_templates, h->stream));
+  TCW_CUDA(h, launch_diff(1, L, h->stream));
+  return TCW_OK;
+}
+
 int tcw_plan_run_host(tcw_handle *h, tcw_plan *p, const float *atoms, tcw_result *results) {
   if (!h || !p) return TCW_ERR_INVALID_ARG;
   if (!atoms || !results) return set_err(h, TCW_ERR_INVALID_ARG, "null host pointer");

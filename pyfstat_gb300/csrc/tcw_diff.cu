@@ -1,0 +1,424 @@
+// Differentiable exponential-window maps: forward values and the adjoint.
+//
+// Per template the tau grid is continuous, tau_n = tau_min + n (tau_max -
+// tau_min) / (N_tau - 1), and the outputs are
+//   lnBtSG    = ln(70 / (N_t0 N_tau)) + logsumexp_mn F_mn            (tcw:196-217)
+//   softmax2F = T logsumexp_mn (2 F_mn / T)        (a smooth max of 2F, T > 0)
+// with gradients with respect to the atoms (a2, b2, ab, Fa, Fb) and to
+// tau_min / tau_max.  Window boundaries move in steps with tau; only the
+// weights are differentiated (the boundaries are piecewise constant).
+//
+// At T = 0.1 the soft-max weights are exp(20 F), so a gradient good to 1e-4
+// needs F to ~1e-9 of its value: this path recomputes the window sums with
+// FP64 recurrences and F in FP64 (the map path stays FP32 / double-word).
+//
+//   pass A (diff_kernel<0>)  per tau column, rows descending: E(j) = x_j +
+//            r E(j+1) for both window edges, F in FP64, online log-sum-exp of
+//            F and 2F/T -> per-tile partials -> finalize per template.
+//   pass B (diff_kernel<1>)  the same walk plus the tau-derivative sums
+//            V(j) = r (V(j+1) + E(j+1)); per cell the adjoint sources
+//            G_c = g dF/dW_c (g = dL/dF) go to per-block scratch (no map is
+//            kept) and g dF/dtau accumulates per column;
+//   pass C (same kernel)     per column, atoms ascending, the transposed
+//            recurrence H(i) = r H(i-1) + sum_{lo(m)=i} G(m)
+//            - sum_{hi(m)+1=i} G(m) r^(L(m)) gives dL/dx(i) = H(i); columns
+//            are reduced across the block and added to the atom gradient.
+// The window-sum factor e^(-k (t_lo - t0)/tau) is left out everywhere: F does
+// not depend on it, so neither do g, dF/dW (in this frame) or dF/dtau.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "../../include/tcw_b200.h"
+#include "tcw_internal.h"
+
+namespace tcw {
+
+namespace {
+
+constexpr float kLog2eF = 1.4426950408889634f;
+
+__device__ __forceinline__ double tau_of(const DiffTemplate &t, uint32_t n) {
+  if (t.N_tau <= 1) return t.tau_min;
+  return t.tau_min + (double)n * ((t.tau_max - t.tau_min) / (double)(t.N_tau - 1u));
+}
+
+// Upper window end for a real tau (the reference's formula with t1 real).
+__device__ __forceinline__ bool exp_hi_real(uint32_t t0, double tau, const Geom &g, uint32_t &hi) {
+  const double t1 = (double)t0 + 3.0 * tau;
+  if (t1 < (double)g.t0_data) return false;
+  const double d = t1 - (double)g.t0_data;
+  const double q = floor((d + (double)g.half) / (double)g.TAtom) - 1.0;
+  const uint32_t b = q < 0.0 ? 0u
+                             : (q >= (double)(g.numAtoms - 1u) ? g.numAtoms - 1u : (uint32_t)q);
+  const double l = floor(d / (double)g.TAtom);
+  const uint32_t last = l >= 4294967295.0 ? 0xFFFFFFFFu : (uint32_t)l;
+  hi = b < last ? b : last;
+  return true;
+}
+
+// F in FP64 with the reference's conditioning test (Rect.cu:93-118).
+struct F64Cell {
+  double F, D;
+  bool ok;
+};
+
+__device__ __forceinline__ F64Cell fstat64(const double W[7]) {
+  const double A = W[0], B = W[1], C = W[2];
+  const double sumAB = A + B, diffAB = A - B;
+  const double disc = sqrt(diffAB * diffAB + 4.0 * C * C);
+  const double denom = sumAB - disc;
+  const double cond = denom > 0.0 ? (sumAB + disc) / denom : INFINITY;
+  F64Cell r{2.0, 0.0, false};
+  if (cond < 1e4) {
+    const double D = A * B - C * C;
+    if (D > 0.0) {
+      const double N = B * (W[3] * W[3] + W[4] * W[4]) + A * (W[5] * W[5] + W[6] * W[6]) -
+                       2.0 * C * (W[3] * W[5] + W[4] * W[6]);
+      r.F = N / D;
+      r.D = D;
+      r.ok = true;
+    }
+  }
+  return r;
+}
+
+// Online log-sum-exp in FP64 (exp in FP64 too: the forward values feed
+// finite-difference checks, where FP32 rounding of the terms would show).
+__device__ __forceinline__ void lse_add(double &m, double &s, double v) {
+  if (v > m) {
+    s = s * exp(m - v) + 1.0;
+    m = v;
+  } else {
+    s += exp(v - m);
+  }
+}
+
+__device__ __forceinline__ void lse_merge(double &m, double &s, double m2, double s2) {
+  if (s2 == 0.0) return;
+  if (s == 0.0) {
+    m = m2;
+    s = s2;
+    return;
+  }
+  const double M = fmax(m, m2);
+  s = s * exp(m - M) + s2 * exp(m2 - M);
+  m = M;
+}
+
+// Blocks of 128 threads, one tau column each; rows of a template all in one tile.
+constexpr int kDiffBlock = 128;
+
+template <int kPass>
+__global__ void __launch_bounds__(kDiffBlock)
+    diff_kernel(const DiffTemplate *__restrict__ T, const DiffItem *__restrict__ items,
+                uint32_t n_items, uint32_t *__restrict__ counter, const float *__restrict__ atoms,
+                const uint32_t *__restrict__ t0s_all, double temp, DiffPartial *__restrict__ parts,
+                const double *__restrict__ lnZ1, const double *__restrict__ lnZ2,
+                const double *__restrict__ gB, const double *__restrict__ gS,
+                float *__restrict__ scratch, uint32_t scratch_rows,
+                double *__restrict__ grad_atoms, double *__restrict__ grad_tau) {
+  __shared__ uint32_t s_item;
+  __shared__ double sh[kDiffBlock / 32][8];
+  __shared__ uint32_t s_end;
+  float *my_scratch = scratch ? scratch + (size_t)blockIdx.x * scratch_rows * 8u * kDiffBlock
+                              : nullptr;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(counter, 1u);
+    __syncthreads();
+    const uint32_t it = s_item;
+    __syncthreads();
+    if (it >= n_items) break;
+    const DiffItem w = items[it];
+    const DiffTemplate t = T[w.tmpl];
+    const uint32_t n = w.n0 + threadIdx.x;
+    const bool active = n < w.n1;
+    const uint32_t *t0s = t0s_all + t.t0_off;
+    const float *x = atoms + t.atom_off * 7u;
+    const double tau = tau_of(t, active ? n : w.n0);
+    const double r1 = exp(-(double)t.g.TAtom / tau), r2 = r1 * r1;
+    double rk[7];
+#pragma unroll
+    for (int c = 0; c < 7; c++) rk[c] = c < 3 ? r2 : r1;
+    const double inv_r1 = r1 > 1e-280 ? 1.0 / r1 : 0.0;
+    // online log-sum-exp (pass A) / tau gradient (pass B)
+    double m1 = -INFINITY, s1 = 0.0, m2 = -INFINITY, s2 = 0.0, dtau = 0.0;
+    double z1 = 0.0, z2 = 0.0, gb = 0.0, gs = 0.0;
+    if (kPass == 1) {
+      // normalisers from the forward outputs: logsumexp F and logsumexp 2F/T
+      z1 = lnZ1[w.tmpl] - log(70.0 / ((double)t.N_t0 * (double)t.N_tau));
+      z2 = lnZ2[w.tmpl] / temp;
+      gb = gB[w.tmpl];
+      gs = gS[w.tmpl];
+    }
+    if (active) {
+      double Elo[7], Ehi[7], Vlo[7], Vhi[7];
+#pragma unroll
+      for (int c = 0; c < 7; c++) Elo[c] = Ehi[c] = Vlo[c] = Vhi[c] = 0.0;
+      uint32_t J = 0, jL = 0, jH = 0, nz = 0xFFFFFFFFu, Lp = 0;
+      double pw = 1.0;
+      bool init = false;
+      for (uint32_t mm = t.N_t0; mm > 0; mm--) {
+        const uint32_t m = mm - 1u;
+        const uint32_t t0 = __ldg(t0s + m);
+        const uint32_t lo = exp_lo(t0, t.g);
+        uint32_t hi = 0;
+        const bool nonempty = exp_hi_real(t0, tau, t.g, hi) && lo <= hi;
+        double G[7] = {0, 0, 0, 0, 0, 0, 0};
+        float p1f = 0.0f;
+        double F = 2.0;
+        if (nonempty) {
+          const uint32_t top = hi + 1u;
+          if (!init || top > J || lo > jL || top > jH) {
+            J = jL = jH = top;
+            nz = 0xFFFFFFFFu;
+#pragma unroll
+            for (int c = 0; c < 7; c++) Elo[c] = Ehi[c] = Vlo[c] = Vhi[c] = 0.0;
+            init = true;
+          }
+          while (jH > top) {
+            jH--;
+#pragma unroll
+            for (int c = 0; c < 7; c++) {
+              const double xv = (double)__ldg(x + (size_t)jH * 7u + c);
+              if (kPass == 1) Vhi[c] = rk[c] * (Vhi[c] + Ehi[c]);
+              Ehi[c] = fma(rk[c], Ehi[c], xv);
+            }
+          }
+          while (jL > lo) {
+            jL--;
+            const float a2 = __ldg(x + (size_t)jL * 7u), b2 = __ldg(x + (size_t)jL * 7u + 1u);
+#pragma unroll
+            for (int c = 0; c < 7; c++) {
+              const double xv = (double)__ldg(x + (size_t)jL * 7u + c);
+              if (kPass == 1) Vlo[c] = rk[c] * (Vlo[c] + Elo[c]);
+              Elo[c] = fma(rk[c], Elo[c], xv);
+            }
+            if (a2 != 0.0f || b2 != 0.0f) nz = jL;
+          }
+          if (nz <= hi) {
+            const uint32_t L = top - lo;
+            if (L != Lp) {
+              if (L == Lp + 1u)
+                pw *= r1;
+              else if (L + 1u == Lp && inv_r1 > 0.0)
+                pw *= inv_r1;
+              else
+                pw = pow(r1, (double)L);
+              Lp = L;
+            }
+            const double p2 = pw * pw;
+            double W[7], V[7];
+#pragma unroll
+            for (int c = 0; c < 7; c++) {
+              const double pk = c < 3 ? p2 : pw;
+              W[c] = Elo[c] - pk * Ehi[c];
+              if (kPass == 1) V[c] = Vlo[c] - pk * (Vhi[c] + (double)L * Ehi[c]);
+            }
+            const F64Cell fc = fstat64(W);
+            F = fc.F;
+            if (kPass == 1 && fc.ok) {
+              const double g = gb * (double)exp2f((float)(F - z1) * kLog2eF) +
+                               gs * 2.0 * (double)exp2f((float)(2.0 * F / temp - z2) * kLog2eF);
+              const double A = W[0], B = W[1], C = W[2], iD = 1.0 / fc.D;
+              const double Fa2 = W[3] * W[3] + W[4] * W[4], Fb2 = W[5] * W[5] + W[6] * W[6];
+              const double re = W[3] * W[5] + W[4] * W[6];
+              double dF[7];
+              dF[0] = (Fb2 - F * B) * iD;
+              dF[1] = (Fa2 - F * A) * iD;
+              dF[2] = (2.0 * F * C - 2.0 * re) * iD;
+              dF[3] = 2.0 * (B * W[3] - C * W[5]) * iD;
+              dF[4] = 2.0 * (B * W[4] - C * W[6]) * iD;
+              dF[5] = 2.0 * (A * W[5] - C * W[3]) * iD;
+              dF[6] = 2.0 * (A * W[6] - C * W[4]) * iD;
+#pragma unroll
+              for (int c = 0; c < 7; c++) {
+                G[c] = g * dF[c];
+                dtau += G[c] * (c < 3 ? 2.0 : 1.0) * V[c];
+              }
+              p1f = (float)pw;
+            }
+          }
+        }
+        if (kPass == 0) {
+          lse_add(m1, s1, F);
+          lse_add(m2, s2, 2.0 * F / temp);
+        } else {
+          float *sc = my_scratch + (size_t)m * 8u * kDiffBlock + threadIdx.x;
+#pragma unroll
+          for (int c = 0; c < 7; c++) sc[(size_t)c * kDiffBlock] = (float)G[c];
+          sc[(size_t)7 * kDiffBlock] = p1f;
+        }
+      }
+    }
+    if (kPass == 0) {
+      // block merge of the two log-sum-exp pairs (warp shuffles, then smem)
+#pragma unroll
+      for (int d = 16; d > 0; d >>= 1) {
+        const double om1 = __shfl_down_sync(0xffffffffu, m1, d);
+        const double os1 = __shfl_down_sync(0xffffffffu, s1, d);
+        const double om2 = __shfl_down_sync(0xffffffffu, m2, d);
+        const double os2 = __shfl_down_sync(0xffffffffu, s2, d);
+        lse_merge(m1, s1, om1, os1);
+        lse_merge(m2, s2, om2, os2);
+      }
+      if ((threadIdx.x & 31u) == 0) {
+        sh[threadIdx.x >> 5][0] = m1;
+        sh[threadIdx.x >> 5][1] = s1;
+        sh[threadIdx.x >> 5][2] = m2;
+        sh[threadIdx.x >> 5][3] = s2;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        for (int k = 1; k < kDiffBlock / 32; k++) {
+          lse_merge(m1, s1, sh[k][0], sh[k][1]);
+          lse_merge(m2, s2, sh[k][2], sh[k][3]);
+        }
+        parts[w.part] = DiffPartial{m1, s1, m2, s2};
+      }
+      __syncthreads();
+      continue;
+    }
+
+    // ---- pass B done for this tile: tau gradient, then pass C (ascending)
+    __syncthreads();  // scratch of all columns written
+    const double scale = active ? (double)t.g.TAtom / (tau * tau) * dtau : 0.0;
+    const double fr = (active && t.N_tau > 1) ? (double)n / (double)(t.N_tau - 1u) : 0.0;
+    double dmax = scale * fr, dmin = scale * (active && t.N_tau > 1 ? 1.0 - fr : (active ? 1.0 : 0.0));
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+      dmax += __shfl_down_sync(0xffffffffu, dmax, d);
+      dmin += __shfl_down_sync(0xffffffffu, dmin, d);
+    }
+    if ((threadIdx.x & 31u) == 0) {
+      sh[threadIdx.x >> 5][0] = dmin;
+      sh[threadIdx.x >> 5][1] = dmax;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double a = 0.0, b = 0.0;
+      for (int k = 0; k < kDiffBlock / 32; k++) {
+        a += sh[k][0];
+        b += sh[k][1];
+      }
+      atomicAdd(grad_tau + 2u * w.tmpl, a);
+      atomicAdd(grad_tau + 2u * w.tmpl + 1u, b);
+      s_end = 0;
+    }
+    __syncthreads();
+    // atom range of the transposed recurrence: from the first row's window
+    // start to the largest window end of the tile
+    const uint32_t i_begin = exp_lo(__ldg(t0s), t.g);
+    uint32_t my_end = i_begin;
+    if (active) {
+      uint32_t hi;
+      if (exp_hi_real(__ldg(t0s + t.N_t0 - 1u), tau, t.g, hi)) my_end = hi + 1u;
+    }
+    atomicMax(&s_end, my_end);
+    __syncthreads();
+    const uint32_t i_end = s_end;
+    double H[7] = {0, 0, 0, 0, 0, 0, 0};
+    uint32_t mi = 0, mr = 0;
+    uint32_t lo_next = exp_lo(__ldg(t0s), t.g);
+    const float *sc0 = my_scratch + threadIdx.x;
+    for (uint32_t i = i_begin; i < i_end; i++) {
+      if (active) {
+#pragma unroll
+        for (int c = 0; c < 7; c++) H[c] *= rk[c];
+        while (mi < t.N_t0 && lo_next <= i) {
+          const float *sc = sc0 + (size_t)mi * 8u * kDiffBlock;
+#pragma unroll
+          for (int c = 0; c < 7; c++) H[c] += (double)sc[(size_t)c * kDiffBlock];
+          mi++;
+          if (mi < t.N_t0) lo_next = exp_lo(__ldg(t0s + mi), t.g);
+        }
+        while (mr < mi) {
+          const uint32_t t0 = __ldg(t0s + mr);
+          uint32_t hi;
+          const uint32_t lo = exp_lo(t0, t.g);
+          uint32_t end = lo;  // empty windows: removal right after injection
+          if (exp_hi_real(t0, tau, t.g, hi) && lo <= hi) end = hi + 1u;
+          if (end > i) break;
+          const float *sc = sc0 + (size_t)mr * 8u * kDiffBlock;
+          const double p1 = (double)sc[(size_t)7 * kDiffBlock], p2 = p1 * p1;
+#pragma unroll
+          for (int c = 0; c < 7; c++) H[c] -= (double)sc[(size_t)c * kDiffBlock] * (c < 3 ? p2 : p1);
+          mr++;
+        }
+      }
+      // reduce the columns' contributions to atom i
+      double v[7];
+#pragma unroll
+      for (int c = 0; c < 7; c++) {
+        v[c] = active ? H[c] : 0.0;
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) v[c] += __shfl_down_sync(0xffffffffu, v[c], d);
+      }
+      if ((threadIdx.x & 31u) == 0) {
+#pragma unroll
+        for (int c = 0; c < 7; c++) sh[threadIdx.x >> 5][c] = v[c];
+      }
+      __syncthreads();
+      if (threadIdx.x < 7u && i < t.g.numAtoms) {
+        double a = 0.0;
+        for (int k = 0; k < kDiffBlock / 32; k++) a += sh[k][threadIdx.x];
+        if (a != 0.0) atomicAdd(grad_atoms + (t.atom_off + i) * 7u + threadIdx.x, a);
+      }
+      __syncthreads();
+    }
+  }
+}
+
+__global__ void diff_finalize_kernel(const DiffTemplate *__restrict__ T, uint32_t n_templates,
+                                     const DiffPartial *__restrict__ parts, double temp,
+                                     double *__restrict__ lnB, double *__restrict__ soft) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n_templates) return;
+  const DiffTemplate t = T[k];
+  double m1 = -INFINITY, s1 = 0.0, m2 = -INFINITY, s2 = 0.0;
+  for (uint32_t p = 0; p < t.n_parts; p++) {
+    const DiffPartial q = parts[t.part_off + p];
+    lse_merge(m1, s1, q.m1, q.s1);
+    lse_merge(m2, s2, q.m2, q.s2);
+  }
+  lnB[k] = log(70.0 / ((double)t.N_t0 * (double)t.N_tau)) + m1 + log(s1);
+  soft[k] = temp * (m2 + log(s2));
+}
+
+}  // namespace
+
+int diff_blocks_per_sm(int pass) {
+  int n = 0;
+  cudaError_t e = pass == 0
+                      ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, diff_kernel<0>, kDiffBlock, 0)
+                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, diff_kernel<1>, kDiffBlock, 0);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    n = 1;
+  }
+  return n > 0 ? n : 1;
+}
+
+cudaError_t launch_diff(int pass, const DiffLaunch &L, cudaStream_t stream) {
+  if (L.n_items == 0) return cudaSuccess;
+  if (pass == 0)
+    diff_kernel<0><<<L.n_blocks, kDiffBlock, 0, stream>>>(
+        L.T, L.items, L.n_items, L.counter, L.atoms, L.t0s, L.temp, L.parts, nullptr, nullptr,
+        nullptr, nullptr, nullptr, 0, nullptr, nullptr);
+  else
+    diff_kernel<1><<<L.n_blocks, kDiffBlock, 0, stream>>>(
+        L.T, L.items, L.n_items, L.counter, L.atoms, L.t0s, L.temp, nullptr, L.lnZ1, L.lnZ2,
+        L.gB, L.gS, L.scratch, L.scratch_rows, L.grad_atoms, L.grad_tau);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_diff_finalize(const DiffTemplate *T, uint32_t n_templates,
+                                 const DiffPartial *parts, double temp, double *lnB, double *soft,
+                                 cudaStream_t stream) {
+  if (n_templates == 0) return cudaSuccess;
+  diff_finalize_kernel<<<(n_templates + 127u) / 128u, 128, 0, stream>>>(T, n_templates, parts,
+                                                                         temp, lnB, soft);
+  return cudaGetLastError();
+}
+
+}  // namespace tcw

@@ -88,4 +88,42 @@ cudaError_t launch_posteriors(const TemplateDev *d_T, const float *d_Fmn, void *
                               double *d_rowsum, double *d_colsum, uint32_t N_t0,
                               uint32_t N_tau, cudaStream_t stream);
 
+// ---------------------------------------------------------------- differentiable path
+// One exponential template with a continuous tau grid (tcw_diff.cu).
+struct DiffTemplate {
+  uint64_t atom_off, t0_off;
+  Geom g;
+  uint32_t N_t0, N_tau;
+  double tau_min, tau_max;
+  uint32_t part_off, n_parts;
+};
+// A tile: columns [n0, n1) (at most 128) of one template, all rows.
+struct DiffItem {
+  uint32_t tmpl, part, n0, n1;
+};
+// Per-tile online log-sum-exp pairs of F and of 2F/T.
+struct DiffPartial {
+  double m1, s1, m2, s2;
+};
+struct DiffLaunch {
+  const DiffTemplate *T;
+  const DiffItem *items;
+  uint32_t n_items, n_blocks;
+  uint32_t *counter;
+  const float *atoms;
+  const uint32_t *t0s;
+  double temp;
+  DiffPartial *parts;                // pass A output
+  const double *lnZ1, *lnZ2, *gB, *gS;  // pass B inputs per template: lnBtSG, softmax2F,
+                                        // dL/dlnBtSG, dL/dsoftmax2F
+  float *scratch;                    // pass B/C: n_blocks x scratch_rows x 8 x 128 floats
+  uint32_t scratch_rows;
+  double *grad_atoms, *grad_tau;     // pass B/C outputs (accumulated; zero them first)
+};
+int diff_blocks_per_sm(int pass);
+cudaError_t launch_diff(int pass, const DiffLaunch &L, cudaStream_t stream);
+cudaError_t launch_diff_finalize(const DiffTemplate *T, uint32_t n_templates,
+                                 const DiffPartial *parts, double temp, double *lnB, double *soft,
+                                 cudaStream_t stream);
+
 }  // namespace tcw
