@@ -61,7 +61,12 @@ class ExpDiffBatch:
         return d
 
     def _stream(self):
-        self.handle.set_stream(torch.cuda.current_stream().cuda_stream)
+        # Run on torch's current stream so that torch reads the outputs in
+        # order.  Torch reports its default stream as handle 0, which the
+        # library takes to mean "the handle's own stream"; 0x1 names the
+        # legacy default stream (cudaStreamLegacy) explicitly.
+        s = torch.cuda.current_stream().cuda_stream
+        self.handle.set_stream(s if s else 0x1)
 
     def forward_raw(self, d_atoms, tau_min, tau_max):
         """(lnBtSG, softmax2F) as FP64 device tensors; d_atoms float32 (rows, 7)."""

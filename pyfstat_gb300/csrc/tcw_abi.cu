@@ -995,7 +995,8 @@ static int diff_prepare(tcw_handle *h, const tcw_diff_desc *desc, uint32_t n,
   S.o_cnt = L.add(sizeof(uint32_t));
   const size_t ctl = L.total;
   S.o_parts = L.add(sizeof(DiffPartial) * S.n_items);
-  S.o_scratch = pass == 1 ? L.add(sizeof(float) * 8u * 128u * (size_t)max_rows * S.n_blocks) : 0;
+  S.o_scratch =
+      pass == 1 ? L.add(sizeof(float) * TCW_DIFF_SLOTS * 128u * (size_t)max_rows * S.n_blocks) : 0;
   S.total = L.total;
   int rc = ensure_ws(h, S.total);
   if (rc) return rc;

@@ -108,6 +108,10 @@ __device__ __forceinline__ void lse_merge(double &m, double &s, double m2, doubl
 
 // Blocks of 128 threads, one tau column each; rows of a template all in one tile.
 constexpr int kDiffBlock = 128;
+// Per-block scratch row of one column: G_c (c = 0..6) and r^L as a float
+// hi/lo pair, so that the removal in the transposed recurrence cancels the
+// injected term to FP64 accuracy.
+constexpr uint32_t kDiffSlots = TCW_DIFF_SLOTS;
 
 template <int kPass>
 __global__ void __launch_bounds__(kDiffBlock)
@@ -121,7 +125,7 @@ __global__ void __launch_bounds__(kDiffBlock)
   __shared__ uint32_t s_item;
   __shared__ double sh[kDiffBlock / 32][8];
   __shared__ uint32_t s_end;
-  float *my_scratch = scratch ? scratch + (size_t)blockIdx.x * scratch_rows * 8u * kDiffBlock
+  float *my_scratch = scratch ? scratch + (size_t)blockIdx.x * scratch_rows * kDiffSlots * kDiffBlock
                               : nullptr;
   for (;;) {
     if (threadIdx.x == 0) s_item = atomicAdd(counter, 1u);
@@ -165,7 +169,7 @@ __global__ void __launch_bounds__(kDiffBlock)
         uint32_t hi = 0;
         const bool nonempty = exp_hi_real(t0, tau, t.g, hi) && lo <= hi;
         double G[7] = {0, 0, 0, 0, 0, 0, 0};
-        float p1f = 0.0f;
+        float p1h = 0.0f, p1l = 0.0f;
         double F = 2.0;
         if (nonempty) {
           const uint32_t top = hi + 1u;
@@ -236,7 +240,8 @@ __global__ void __launch_bounds__(kDiffBlock)
                 G[c] = g * dF[c];
                 dtau += G[c] * (c < 3 ? 2.0 : 1.0) * V[c];
               }
-              p1f = (float)pw;
+              p1h = (float)pw;
+              p1l = (float)(pw - (double)p1h);
             }
           }
         }
@@ -244,10 +249,11 @@ __global__ void __launch_bounds__(kDiffBlock)
           lse_add(m1, s1, F);
           lse_add(m2, s2, 2.0 * F / temp);
         } else {
-          float *sc = my_scratch + (size_t)m * 8u * kDiffBlock + threadIdx.x;
+          float *sc = my_scratch + (size_t)m * kDiffSlots * kDiffBlock + threadIdx.x;
 #pragma unroll
           for (int c = 0; c < 7; c++) sc[(size_t)c * kDiffBlock] = (float)G[c];
-          sc[(size_t)7 * kDiffBlock] = p1f;
+          sc[(size_t)7 * kDiffBlock] = p1h;
+          sc[(size_t)8 * kDiffBlock] = p1l;
         }
       }
     }
@@ -326,7 +332,7 @@ __global__ void __launch_bounds__(kDiffBlock)
 #pragma unroll
         for (int c = 0; c < 7; c++) H[c] *= rk[c];
         while (mi < t.N_t0 && lo_next <= i) {
-          const float *sc = sc0 + (size_t)mi * 8u * kDiffBlock;
+          const float *sc = sc0 + (size_t)mi * kDiffSlots * kDiffBlock;
 #pragma unroll
           for (int c = 0; c < 7; c++) H[c] += (double)sc[(size_t)c * kDiffBlock];
           mi++;
@@ -339,8 +345,9 @@ __global__ void __launch_bounds__(kDiffBlock)
           uint32_t end = lo;  // empty windows: removal right after injection
           if (exp_hi_real(t0, tau, t.g, hi) && lo <= hi) end = hi + 1u;
           if (end > i) break;
-          const float *sc = sc0 + (size_t)mr * 8u * kDiffBlock;
-          const double p1 = (double)sc[(size_t)7 * kDiffBlock], p2 = p1 * p1;
+          const float *sc = sc0 + (size_t)mr * kDiffSlots * kDiffBlock;
+          const double p1 = (double)sc[(size_t)7 * kDiffBlock] + (double)sc[(size_t)8 * kDiffBlock];
+          const double p2 = p1 * p1;
 #pragma unroll
           for (int c = 0; c < 7; c++) H[c] -= (double)sc[(size_t)c * kDiffBlock] * (c < 3 ? p2 : p1);
           mr++;

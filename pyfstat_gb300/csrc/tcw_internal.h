@@ -102,6 +102,9 @@ struct DiffItem {
   uint32_t tmpl, part, n0, n1;
 };
 // Per-tile online log-sum-exp pairs of F and of 2F/T.
+// floats per column and t0 row in the backward pass's per-block scratch
+#define TCW_DIFF_SLOTS 9u
+
 struct DiffPartial {
   double m1, s1, m2, s2;
 };
@@ -116,7 +119,7 @@ struct DiffLaunch {
   DiffPartial *parts;                // pass A output
   const double *lnZ1, *lnZ2, *gB, *gS;  // pass B inputs per template: lnBtSG, softmax2F,
                                         // dL/dlnBtSG, dL/dsoftmax2F
-  float *scratch;                    // pass B/C: n_blocks x scratch_rows x 8 x 128 floats
+  float *scratch;                    // pass B/C: n_blocks x scratch_rows x TCW_DIFF_SLOTS x 128 floats
   uint32_t scratch_rows;
   double *grad_atoms, *grad_tau;     // pass B/C outputs (accumulated; zero them first)
 };

@@ -58,8 +58,8 @@ def test_values_and_gradients_match_torch_fp64_reference(torch_cuda):
         a = torch.tensor(t["tau_min"], dtype=torch.float64, requires_grad=True)
         b = torch.tensor(t["tau_max"], dtype=torch.float64, requires_grad=True)
         rl, rs, _ = R.stats(x, 1800, t["t0_data"], t["t0s"], a, b, t["N_tau"], T)
-        assert float(lnB[k]) == pytest.approx(float(rl), rel=1e-9)
-        assert float(soft[k]) == pytest.approx(float(rs), rel=1e-9)
+        assert float(lnB[k].detach()) == pytest.approx(float(rl), rel=1e-9)
+        assert float(soft[k].detach()) == pytest.approx(float(rs), rel=1e-9)
         (rl * float(gl[k]) + rs * float(gs[k])).backward()
         n = t["atoms"].shape[0]
         g_ref = x.grad.numpy()
@@ -161,4 +161,6 @@ def test_differentiation_workload_256x2000x1024sq(torch_cuda):
         _, sp = batch.forward_raw(atoms, tmin, p)
         _, sm = batch.forward_raw(atoms, tmin, m)
         fd = (float(sp[k]) - float(sm[k])) / (2 * h)
+        print(f"template {k}: d softmax2F / d tau_max adjoint {float(gt[k, 1]):.9e}, "
+              f"central FD {fd:.9e}")
         assert fd == pytest.approx(float(gt[k, 1]), rel=1e-4, abs=1e-12)

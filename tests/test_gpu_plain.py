@@ -119,7 +119,8 @@ def test_device_pointer_entry_on_torch_stream(lib, handle, oracle):
     taus = torch.from_numpy(c["taus"].astype(np.int32)).to(dev)
     Fmn = torch.empty((len(c["t0s"]), len(c["taus"])), dtype=torch.float32, device=dev)
     res = torch.zeros(5, dtype=torch.float64, device=dev)  # 40-byte tcw_result
-    handle.set_stream(torch.cuda.current_stream().cuda_stream)
+    # torch's default stream is handle 0; 0x1 (cudaStreamLegacy) names it for the library
+    handle.set_stream(torch.cuda.current_stream().cuda_stream or 0x1)
     try:
         handle.map_plain(A, A.shape[0], 1800, c["t0_data"], 1, t0s, len(c["t0s"]), taus,
                          len(c["taus"]), Fmn, res, flags=FLAGS_ALL)
