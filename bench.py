@@ -35,7 +35,10 @@ UNIT = "cells/s"
 # compensation not counted): FP32 flops (an FMA counts 2) and MUFU ops.
 FLOPS_PER_CELL = {1: 34.0, 2: 55.0}
 MUFU_PER_CELL = 3.0
-TRAFFIC_FILE = os.path.join(REPO, "profiles", "map_kernel_batched4096.md")
+# ncu summaries of the map kernels on this workload; each holds a line
+# "traffic_bytes_per_launch = N" (DRAM read + write bytes of one launch)
+TRAFFIC_FILES = {"rect_map_kernel": os.path.join(REPO, "profiles", "rect_map_kernel_batched.md"),
+                 "exp_map_kernel": os.path.join(REPO, "profiles", "exp_map_kernel_batched.md")}
 
 
 def parse():
@@ -165,16 +168,22 @@ def cpu_baseline(templates, seconds, threads):
     return cells / dt, cells, used, dt
 
 
-def traffic_per_launch():
-    """DRAM bytes per map-kernel launch from the committed ncu summary, if any."""
+def traffic_per_launch(kernel):
+    """DRAM bytes per launch of a map kernel from its committed ncu summary, if any."""
     try:
-        with open(TRAFFIC_FILE) as f:
+        with open(TRAFFIC_FILES[kernel]) as f:
             for line in f:
                 if line.strip().startswith("traffic_bytes_per_launch"):
                     return float(line.split("=")[1].split()[0])
-    except (OSError, ValueError, IndexError):
+    except (OSError, ValueError, IndexError, KeyError):
         pass
     return None
+
+
+def launches_per_step(n_rect, n_exp):
+    """Kernels one plan step launches: prefix (rect templates), repack and
+    map (exp templates), map (rect templates), finalize."""
+    return (2 if n_rect else 0) + (2 if n_exp else 0) + 1
 
 
 # ------------------------------------------------------------------ arms
@@ -358,7 +367,7 @@ def run_ours(args, ws, rank, local):
         "peak": peaks["fp32_tflops"] if bound == "fp32" else peaks["mufu_tops"],
         "unit": "TFLOP/s" if bound == "fp32" else "Tops/s",
         "frac": d["fp32_frac"] if bound == "fp32" else d["mufu_frac"],
-        "traffic": traffic_per_launch(),
+        "traffic": traffic_per_launch(dom),
         "kernel": dom,
         "kernels": per_kernel, "prefix_ms": prefix_ms, "finalize_ms": fin_ms,
         "peak_source": "measured on this GPU by tcw_probe_peaks (FMA chains / ex2 chains), "
@@ -401,7 +410,7 @@ def run_ours(args, ws, rank, local):
                 "d2h_bytes_per_step": 40 * n_t,
                 "api": "TransientMapBatch.run (tcw_plan_run_host), pinned host atoms"},
         "plain_per_template": plain,
-        "gpu_launches": 3 * args.steps,
+        "gpu_launches": launches_per_step(n_rect, n_t - n_rect) * args.steps,
         "clocks": clk,
     }
     print(json.dumps(line), flush=True)

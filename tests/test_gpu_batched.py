@@ -142,3 +142,24 @@ def test_single_cell_and_single_atom_templates(oracle):
         t = templates[k]
         F64, _ = oracle_reference(oracle, t)
         assert float(res["maxF"][k]) == pytest.approx(F64[0, 0], rel=REL_TOL)
+
+
+def test_autotuned_plan_matches_default_plan(tmp_path, monkeypatch):
+    monkeypatch.setenv("PYFSTAT_GB300_TUNE_CACHE", str(tmp_path / "tiles.json"))
+    tl = small_templates(n=32, seed=9)
+    ref = TransientMapBatch(tl)
+    tuned = TransientMapBatch(tl, tile_config="auto", handle=ref.handle)
+    cfg = tuned.tile_config
+    assert cfg["rect_tm"] in (32, 64, 128) and cfg["exp_tn"] in (32, 64, 128)
+    a, b = ref.run(), tuned.run()
+    rect = ref.desc["window"] == 1
+    assert np.array_equal(a["maxF"][rect], b["maxF"][rect])
+    np.testing.assert_allclose(b["maxF"], a["maxF"], rtol=2e-6)
+    # exp cells round differently under another chunking (<= 2e-6 relative),
+    # and the log-sum-exp partial sums are merged in another order
+    np.testing.assert_allclose(b["lnBtSG"], a["lnBtSG"], rtol=2e-6)
+    # a second construction reads the cache
+    again = TransientMapBatch(tl, tile_config="auto", handle=ref.handle)
+    assert again.tile_config == cfg
+    for x in (again, tuned, ref):
+        x.close()
