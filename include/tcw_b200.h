@@ -183,6 +183,20 @@ int tcw_expdiff_backward(tcw_handle *h, const tcw_diff_desc *desc, uint32_t n_te
                          const double *d_grad_lnBtSG, const double *d_grad_softmax2F,
                          double *d_grad_atoms, uint64_t n_atom_rows, double *d_grad_tau);
 
+/* Full-FP64 map by direct summation over each cell's window (FP64 weights
+ * and sums, FP64 F with the reference's conditioning test, no recurrence and
+ * no compensation): the GPU reference for precision reports.  Device
+ * atoms/grids as in tcw_map_plain; `rows` is a HOST list of n_rows t0 indices
+ * (each < N_t0; NULL = all rows, then n_rows == N_t0).  Writes
+ * d_F[r * N_tau + n] for the r-th listed row, and the condition number to
+ * d_cond (nullable).  Cost: one FP64 FMA per channel per atom of each window.
+ * A precision utility; it has no counterpart in the reference, whose own
+ * FP64 path is the 'lal' version (tcw:547-587). */
+int tcw_map_f64(tcw_handle *h, const float *d_atoms, uint32_t numAtoms, uint32_t TAtom,
+                uint32_t t0_data, int window, const uint32_t *d_t0s, uint32_t N_t0,
+                const uint32_t *d_taus, uint32_t N_tau, const uint32_t *rows, uint32_t n_rows,
+                double *d_F, double *d_cond);
+
 /* Measured throughput of `device` for roofline denominators: FP32 and FP64
  * FMA in TFLOP/s (an FMA counts 2), MUFU ex2 in Tops/s, FP32 through packed
  * f32x2 FMAs in TFLOP/s.  A measurement utility; it has no counterpart in the

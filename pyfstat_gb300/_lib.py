@@ -99,6 +99,8 @@ SIGNATURES = {
     "tcw_debug_fail_alloc": (ctypes.c_int, [_vp, ctypes.c_int]),
     "tcw_map_plain_noalloc": (ctypes.c_int, [_vp, _vp, _c_u32, _c_u32, _c_u32, ctypes.c_int, _vp,
                                              _c_u32, _vp, _c_u32, _vp, _vp, ctypes.c_int]),
+    "tcw_map_f64": (ctypes.c_int, [_vp, _vp, _c_u32, _c_u32, _c_u32, ctypes.c_int, _vp, _c_u32,
+                                   _vp, _c_u32, _vp, _c_u32, _vp, _vp]),
     "tcw_expdiff_forward": (ctypes.c_int, [_vp, _vp, _c_u32, _vp, _vp, _c_u64, ctypes.c_double,
                                            _vp, _vp]),
     "tcw_expdiff_backward": (ctypes.c_int, [_vp, _vp, _c_u32, _vp, _vp, _c_u64, ctypes.c_double,
@@ -263,6 +265,21 @@ class Handle:
         rc = load().tcw_map_plain(self.ptr, _p(d_atoms), int(numAtoms), int(TAtom),
                                   int(t0_data), int(window), _p(d_t0s), int(N_t0), _p(d_taus),
                                   int(N_tau), _p(d_Fmn), _p(d_result), int(flags))
+        check(rc, self.ptr)
+
+    def map_f64(self, d_atoms, numAtoms, TAtom, t0_data, window, d_t0s, N_t0, d_taus, N_tau,
+                d_F, rows=None, d_cond=None):
+        """Full-FP64 direct-summation map of the listed t0 rows (host indices;
+        None = all rows) into device FP64 ``d_F`` (n_rows x N_tau); asynchronous
+        on the handle's stream."""
+        if rows is None:
+            rp, nr = None, int(N_t0)
+        else:
+            rows = np.ascontiguousarray(rows, dtype=np.uint32)
+            rp, nr = rows.ctypes.data, rows.shape[0]
+        rc = load().tcw_map_f64(self.ptr, _p(d_atoms), int(numAtoms), int(TAtom), int(t0_data),
+                                int(window), _p(d_t0s), int(N_t0), _p(d_taus), int(N_tau), rp, nr,
+                                _p(d_F), _p(d_cond))
         check(rc, self.ptr)
 
 

@@ -1106,4 +1106,45 @@ int tcw_plan_run_host(tcw_handle *h, tcw_plan *p, const float *atoms, tcw_result
   return TCW_OK;
 }
 
+int tcw_map_f64(tcw_handle *h, const float *d_atoms, uint32_t numAtoms, uint32_t TAtom,
+                uint32_t t0_data, int window, const uint32_t *d_t0s, uint32_t N_t0,
+                const uint32_t *d_taus, uint32_t N_tau, const uint32_t *rows, uint32_t n_rows,
+                double *d_F, double *d_cond) {
+  if (!h) return TCW_ERR_INVALID_ARG;
+  if (!d_atoms || !d_t0s || !d_taus || !d_F)
+    return set_err(h, TCW_ERR_INVALID_ARG, "null device pointer");
+  if (!valid_window(window))
+    return set_err(h, TCW_ERR_INVALID_ARG,
+                   "invalid window type %d: TCW_WINDOW_RECT or TCW_WINDOW_EXP", window);
+  int rc = check_geometry(h, numAtoms, TAtom, t0_data, N_t0, N_tau);
+  if (rc) return rc;
+  if (!rows && n_rows != N_t0)
+    return set_err(h, TCW_ERR_INVALID_ARG, "without a row list n_rows must equal N_t0");
+  if (n_rows == 0) return set_err(h, TCW_ERR_INVALID_ARG, "no rows requested");
+  if (rows)
+    for (uint32_t k = 0; k < n_rows; k++)
+      if (rows[k] >= N_t0)
+        return set_err(h, TCW_ERR_INVALID_ARG, "row %u (entry %u) outside the t0 grid of %u",
+                       rows[k], k, N_t0);
+  rc = set_device(h);
+  if (rc) return rc;
+  const uint32_t *d_rows = nullptr;
+  if (rows) {
+    const size_t bytes = sizeof(uint32_t) * (size_t)n_rows;
+    rc = ensure_ws(h, bytes);
+    if (rc) return rc;
+    rc = ensure_stage(h, bytes);
+    if (rc) return rc;
+    memcpy(h->h_stage, rows, bytes);
+    TCW_CUDA(h, cudaMemcpyAsync(h->d_ws, h->h_stage, bytes, cudaMemcpyHostToDevice, h->stream));
+    TCW_CUDA(h, cudaEventRecord(h->stage_ev, h->stream));
+    h->stage_pending = true;
+    d_rows = reinterpret_cast<const uint32_t *>(h->d_ws);
+  }
+  const Geom g = make_geom(numAtoms, TAtom, t0_data);
+  TCW_CUDA(h, launch_map_f64(window, d_atoms, g, d_t0s, d_taus, N_tau, d_rows, n_rows, d_F,
+                             d_cond, h->stream));
+  return TCW_OK;
+}
+
 }  // extern "C"

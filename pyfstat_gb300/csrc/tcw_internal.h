@@ -125,6 +125,11 @@ struct DiffLaunch {
 };
 int diff_blocks_per_sm(int pass);
 cudaError_t launch_diff(int pass, const DiffLaunch &L, cudaStream_t stream);
+// Full-FP64 direct-summation map of rows rows[0..n_rows) (all rows when rows
+// is NULL) into F[r * N_tau + n]; cond optional.
+cudaError_t launch_map_f64(int window, const float *atoms, const Geom &g, const uint32_t *t0s,
+                           const uint32_t *taus, uint32_t N_tau, const uint32_t *rows,
+                           uint32_t n_rows, double *F, double *cond, cudaStream_t stream);
 cudaError_t launch_diff_finalize(const DiffTemplate *T, uint32_t n_templates,
                                  const DiffPartial *parts, double temp, double *lnB, double *soft,
                                  cudaStream_t stream);

@@ -141,3 +141,22 @@ def batched_templates(n_templates=4096, seed=12345, nsft_range=(200, 4000),
                         t0_data=t0_data, t0=t0_data, dt0=dt0, tau=Tsft, dtau=dtau,
                         N_t0=N_t0, N_tau=N_tau))
     return out
+
+
+def precision_templates(n_templates=64, seed=777, nsft=17532, ndet=2, gap_frac=0.05,
+                        N_t0=8192, N_tau=4096, Tsft=TSFT_DEFAULT):
+    """Precision-at-scale workload: ``n_templates`` exponential-window
+    templates of one year of data (17532 SFTs of 1800 s per detector, two
+    detectors merged, 5 % of SFTs dropped as gaps), each on an 8192 t0 x 4096
+    tau grid covering the span: ``dt0 = span // N_t0``,
+    ``tau = Tsft + n * dtau`` with ``dtau = (span - Tsft) // (N_tau - 1)``.
+    Template k uses atoms seed ``seed + k``."""
+    out = []
+    for k in range(n_templates):
+        t0_data, atoms = merged_atoms(seed + k, nsft, ndet, Tsft, gap_frac=gap_frac)
+        span = atoms.shape[0] * Tsft
+        out.append(dict(window=2, atoms=atoms, TAtom=Tsft, t0_data=t0_data, t0=t0_data,
+                        dt0=max(1, span // N_t0), tau=Tsft,
+                        dtau=max(1, (span - Tsft) // max(1, N_tau - 1)), N_t0=N_t0,
+                        N_tau=N_tau))
+    return out
