@@ -48,6 +48,8 @@ extern "C" {
 #define TCW_ERR_TIMEOUT (-5)
 #define TCW_ERR_UNSUPPORTED (-6)
 #define TCW_ERR_OVERFLOW (-7)
+#define TCW_ERR_IO (-8)      /* file could not be opened, read or written */
+#define TCW_ERR_FORMAT (-9)  /* malformed line in a text file */
 
 /* window types: lalpulsar's transientWindowType_t values */
 #define TCW_WINDOW_NONE 0
@@ -139,10 +141,17 @@ int tcw_plan_info(const tcw_plan *plan, uint64_t *n_cells, uint32_t *n_items,
 /* use_graph != 0: the first run captures the launch sequence into a CUDA
  * graph owned by the plan; later runs replay it (same d_atoms/d_results
  * pointers required; different pointers re-capture).  On the legacy default
- * stream (set_stream(NULL stream)) runs are launched without a graph. */
+ * stream (cudaStreamLegacy) runs are launched without a graph. */
 int tcw_plan_run(tcw_handle *h, tcw_plan *plan, const float *d_atoms, tcw_result *d_results,
                  int use_graph);
 int tcw_plan_run_host(tcw_handle *h, tcw_plan *plan, const float *atoms, tcw_result *results);
+/* As tcw_plan_run, and also writes every template's FP32 map: template k's
+ * (N_t0, N_tau) row-major map starts at d_maps + sum_{j<k} N_t0(j) N_tau(j)
+ * (descriptor order; tcw_plan_info's n_cells floats in all).  Replaces the
+ * per-template map downloads of the reference's callers (tcw:810-815 and
+ * core.py:1534-1540 read cells of full maps). */
+int tcw_plan_run_maps(tcw_handle *h, tcw_plan *plan, const float *d_atoms, tcw_result *d_results,
+                      float *d_maps, int use_graph);
 /* One run without a graph and with the two map kernels one after the other,
  * CUDA events between the kernels on the handle's stream; synchronises and
  * writes the durations (ms) of the prefix, rectangular-map, exponential-map
@@ -196,6 +205,30 @@ int tcw_map_f64(tcw_handle *h, const float *d_atoms, uint32_t numAtoms, uint32_t
                 uint32_t t0_data, int window, const uint32_t *d_t0s, uint32_t N_t0,
                 const uint32_t *d_taus, uint32_t N_tau, const uint32_t *rows, uint32_t n_rows,
                 double *d_F, double *d_cond);
+
+/* ---- file formats (host only, no device or handle) ---- */
+
+/* Text map body in the lalpulsar write_transientFstatMap_to_fp layout, one
+ * line "  %10d %10d %- 11.8g\n" of (t0s[m], taus[n], 2 F[m, n]) per cell in
+ * row-major order; header lines are the caller's (append != 0 appends).
+ * Replaces the Python line loop of write_F_mn_to_file (tcw:289-317). */
+int tcw_write_map_text(const char *path, const float *F, uint32_t N_t0, uint32_t N_tau,
+                       const uint32_t *t0s, const uint32_t *taus, int append);
+/* Columns (t0, tau, 2F) of a text map ('#' comment lines skipped), as read by
+ * read_from_file (tcw:159-184).  With NULL outputs only counts the lines into
+ * *n_lines; otherwise fills up to `capacity` lines (TCW_ERR_OVERFLOW beyond). */
+int tcw_read_map_text(const char *path, uint64_t *n_lines, double *t0, double *tau, double *twoF,
+                      uint64_t capacity);
+/* F-statistic atoms text ('%' comment lines skipped; columns tGPS a2 b2 ab
+ * Fa_re Fa_im Fb_re Fb_im, the file of core.py:1879-1910 as checked by
+ * tests/test_core.py:811-826): timestamps and (n, 7) float32 rows, two-call
+ * pattern as tcw_read_map_text. */
+int tcw_read_atoms_text(const char *path, uint64_t *n_rows, uint32_t *timestamps, float *atoms7,
+                        uint64_t capacity);
+/* Writes atoms in the same column layout (header line "%% tGPS a2 b2 ab
+ * Fa_re Fa_im Fb_re Fb_im", values with 9 significant digits). */
+int tcw_write_atoms_text(const char *path, const uint32_t *timestamps, const float *atoms7,
+                         uint64_t n_rows, int append);
 
 /* Measured throughput of `device` for roofline denominators: FP32 and FP64
  * FMA in TFLOP/s (an FMA counts 2), MUFU ex2 in Tops/s, FP32 through packed

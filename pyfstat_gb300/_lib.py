@@ -20,6 +20,8 @@ TCW_ERR_ALLOC = -4
 TCW_ERR_TIMEOUT = -5
 TCW_ERR_UNSUPPORTED = -6
 TCW_ERR_OVERFLOW = -7
+TCW_ERR_IO = -8
+TCW_ERR_FORMAT = -9
 
 TCW_WINDOW_NONE = 0
 TCW_WINDOW_RECT = 1
@@ -94,6 +96,7 @@ SIGNATURES = {
     "tcw_plan_info": (ctypes.c_int, [_vp, ctypes.POINTER(_c_u64), ctypes.POINTER(_c_u32),
                                      ctypes.POINTER(_c_u64), ctypes.POINTER(TcwTileConfig)]),
     "tcw_plan_run": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int]),
+    "tcw_plan_run_maps": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, ctypes.c_int]),
     "tcw_plan_run_host": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
     "tcw_plan_run_timed": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.POINTER(ctypes.c_float)]),
     "tcw_debug_fail_alloc": (ctypes.c_int, [_vp, ctypes.c_int]),
@@ -105,6 +108,13 @@ SIGNATURES = {
                                            _vp, _vp]),
     "tcw_expdiff_backward": (ctypes.c_int, [_vp, _vp, _c_u32, _vp, _vp, _c_u64, ctypes.c_double,
                                             _vp, _vp, _vp, _vp, _vp, _c_u64, _vp]),
+    "tcw_write_map_text": (ctypes.c_int, [ctypes.c_char_p, _vp, _c_u32, _c_u32, _vp, _vp,
+                                          ctypes.c_int]),
+    "tcw_read_map_text": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_c_u64), _vp, _vp, _vp,
+                                         _c_u64]),
+    "tcw_read_atoms_text": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_c_u64), _vp, _vp,
+                                           _c_u64]),
+    "tcw_write_atoms_text": (ctypes.c_int, [ctypes.c_char_p, _vp, _vp, _c_u64, ctypes.c_int]),
     "tcw_probe_peaks": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                        ctypes.POINTER(ctypes.c_double),
                                        ctypes.POINTER(ctypes.c_double),
@@ -343,6 +353,13 @@ class Plan:
     def run(self, d_atoms, d_results, use_graph=True):
         check(load().tcw_plan_run(self.handle.ptr, self._p, _p(d_atoms), _p(d_results),
                                   int(bool(use_graph))), self.handle.ptr)
+
+    def run_maps(self, d_atoms, d_results, d_maps, use_graph=True):
+        """As :meth:`run`, also writing all templates' FP32 maps into ``d_maps``
+        (``n_cells`` floats; template k's map at the sum of the earlier
+        templates' N_t0 * N_tau, row-major)."""
+        check(load().tcw_plan_run_maps(self.handle.ptr, self._p, _p(d_atoms), _p(d_results),
+                                       _p(d_maps), int(bool(use_graph))), self.handle.ptr)
 
     def run_timed(self, d_atoms, d_results):
         """One run with per-kernel CUDA events: (prefix, rect map, exp map, finalize) ms."""

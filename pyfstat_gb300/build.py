@@ -16,7 +16,7 @@ LIB_NAME = "libtcw_b200.so"
 LIB_PATH = os.path.join(HERE, LIB_NAME)
 BUILD_DIR = os.path.join(HERE, "_build")
 SOURCES = ("tcw_kernels.cu", "tcw_abi.cu", "tcw_probe.cu", "tcw_noalloc.cu", "tcw_diff.cu",
-           "tcw_f64.cu")
+           "tcw_f64.cu", "tcw_io.cpp")
 HEADERS = ("tcw_cell.h", "tcw_internal.h")
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 

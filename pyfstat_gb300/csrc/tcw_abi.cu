@@ -59,6 +59,7 @@ struct tcw_plan {
   cudaGraphExec_t gexec = nullptr;
   const float *g_atoms = nullptr;
   tcw_result *g_results = nullptr;
+  float *g_maps = nullptr;
   cudaStream_t g_stream = nullptr;
   // buffers of the host-buffer entry point
   float *d_atoms_in = nullptr;
@@ -303,6 +304,8 @@ const char *tcw_strerror(int status) {
     case TCW_ERR_TIMEOUT: return "timed out waiting for the device";
     case TCW_ERR_UNSUPPORTED: return "unsupported";
     case TCW_ERR_OVERFLOW: return "size or time range overflow";
+    case TCW_ERR_IO: return "file input/output error";
+    case TCW_ERR_FORMAT: return "malformed line in a text file";
     default: return "unknown status";
   }
 }
@@ -694,6 +697,7 @@ int tcw_plan_create(tcw_handle *h, const tcw_template_desc *desc, uint32_t n_tem
       t.atom_off = d.atom_offset;
       t.t0_off = d.t0_offset;
       t.tau_off = d.tau_offset;
+      t.map_off = cells;  // maps of tcw_plan_run_maps: templates in descriptor order
       if (d.window == TCW_WINDOW_RECT) {
         t.p_off = p_rows;
         p_rows += (uint64_t)d.numAtoms + 1u;
@@ -828,7 +832,7 @@ int tcw_plan_info(const tcw_plan *p, uint64_t *n_cells, uint32_t *n_items,
 }
 
 static MapLaunch plan_launch(const tcw_handle *h, const tcw_plan *p, int window,
-                             const float *d_atoms) {
+                             const float *d_atoms, float *d_maps) {
   MapLaunch ml{};
   const bool rect = window == TCW_WINDOW_RECT;
   ml.T = p->d_T;
@@ -837,7 +841,7 @@ static MapLaunch plan_launch(const tcw_handle *h, const tcw_plan *p, int window,
   ml.counter = p->d_counter + (rect ? 0 : 1);
   ml.n_blocks = rect ? p->n_blocks_rect : p->n_blocks_exp;
   ml.persistent = true;
-  ml.write_map = false;
+  ml.write_map = d_maps != nullptr;
   ml.prec = p->prec;
   ml.priority = rect ? h->prio_low : h->prio_high;
   ml.atoms = d_atoms;
@@ -845,7 +849,7 @@ static MapLaunch plan_launch(const tcw_handle *h, const tcw_plan *p, int window,
   ml.t0s = p->d_t0s;
   ml.taus = p->d_taus;
   ml.P = p->d_P;
-  ml.Fmn = nullptr;
+  ml.Fmn = d_maps;
   ml.parts = p->d_parts;
   return ml;
 }
@@ -853,15 +857,17 @@ static MapLaunch plan_launch(const tcw_handle *h, const tcw_plan *p, int window,
 // prefix -> (exp tiles on the main stream at high priority || rect tiles on
 // the side stream) -> finalize.  The exp tiles are the long ones; the rect
 // kernel's blocks fill SMs as exp blocks retire.
-static int plan_enqueue(tcw_handle *h, tcw_plan *p, const float *d_atoms, tcw_result *d_results) {
+static int plan_enqueue(tcw_handle *h, tcw_plan *p, const float *d_atoms, tcw_result *d_results,
+                        float *d_maps) {
   TCW_CUDA(h, cudaMemsetAsync(p->d_counter, 0, 2 * sizeof(uint32_t), h->stream));
   TCW_CUDA(h, launch_prefix(p->d_T, p->d_rect_list, p->n_rect, d_atoms, p->d_P, p->prec,
                             h->stream));
   TCW_CUDA(h, cudaEventRecord(h->fork_ev, h->stream));
   TCW_CUDA(h, cudaStreamWaitEvent(h->side_stream, h->fork_ev, 0));
   TCW_CUDA(h, launch_repack(p->d_T, p->d_exp_list, p->n_exp, d_atoms, p->d_A8, h->stream));
-  TCW_CUDA(h, launch_map(TCW_WINDOW_EXP, plan_launch(h, p, TCW_WINDOW_EXP, d_atoms), h->stream));
-  TCW_CUDA(h, launch_map(TCW_WINDOW_RECT, plan_launch(h, p, TCW_WINDOW_RECT, d_atoms),
+  TCW_CUDA(h, launch_map(TCW_WINDOW_EXP, plan_launch(h, p, TCW_WINDOW_EXP, d_atoms, d_maps),
+                         h->stream));
+  TCW_CUDA(h, launch_map(TCW_WINDOW_RECT, plan_launch(h, p, TCW_WINDOW_RECT, d_atoms, d_maps),
                          h->side_stream));
   TCW_CUDA(h, cudaEventRecord(h->join_ev, h->side_stream));
   TCW_CUDA(h, cudaStreamWaitEvent(h->stream, h->join_ev, 0));
@@ -869,8 +875,10 @@ static int plan_enqueue(tcw_handle *h, tcw_plan *p, const float *d_atoms, tcw_re
   return TCW_OK;
 }
 
-int tcw_plan_run(tcw_handle *h, tcw_plan *p, const float *d_atoms, tcw_result *d_results,
-                 int use_graph) {
+}  // extern "C"
+
+static int plan_run(tcw_handle *h, tcw_plan *p, const float *d_atoms, tcw_result *d_results,
+                    float *d_maps, int use_graph) {
   if (!h || !p) return TCW_ERR_INVALID_ARG;
   if (!d_atoms || !d_results) return set_err(h, TCW_ERR_INVALID_ARG, "null device pointer");
   if (p->device != h->device)
@@ -878,15 +886,16 @@ int tcw_plan_run(tcw_handle *h, tcw_plan *p, const float *d_atoms, tcw_result *d
   int rc = set_device(h);
   if (rc) return rc;
   // stream capture is not allowed on the legacy default stream: run directly
-  if (!use_graph || h->stream == nullptr) return plan_enqueue(h, p, d_atoms, d_results);
-  if (!p->gexec || p->g_atoms != d_atoms || p->g_results != d_results ||
+  if (!use_graph || h->stream == nullptr || h->stream == cudaStreamLegacy)
+    return plan_enqueue(h, p, d_atoms, d_results, d_maps);
+  if (!p->gexec || p->g_atoms != d_atoms || p->g_results != d_results || p->g_maps != d_maps ||
       p->g_stream != h->stream) {
     if (p->gexec) {
       cudaGraphExecDestroy(p->gexec);
       p->gexec = nullptr;
     }
     TCW_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    rc = plan_enqueue(h, p, d_atoms, d_results);
+    rc = plan_enqueue(h, p, d_atoms, d_results, d_maps);
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
     if (rc) {
@@ -902,10 +911,24 @@ int tcw_plan_run(tcw_handle *h, tcw_plan *p, const float *d_atoms, tcw_result *d
     }
     p->g_atoms = d_atoms;
     p->g_results = d_results;
+    p->g_maps = d_maps;
     p->g_stream = h->stream;
   }
   TCW_CUDA(h, cudaGraphLaunch(p->gexec, h->stream));
   return TCW_OK;
+}
+
+extern "C" {
+
+int tcw_plan_run(tcw_handle *h, tcw_plan *p, const float *d_atoms, tcw_result *d_results,
+                 int use_graph) {
+  return plan_run(h, p, d_atoms, d_results, nullptr, use_graph);
+}
+
+int tcw_plan_run_maps(tcw_handle *h, tcw_plan *p, const float *d_atoms, tcw_result *d_results,
+                      float *d_maps, int use_graph) {
+  if (h && !d_maps) return set_err(h, TCW_ERR_INVALID_ARG, "null map buffer");
+  return plan_run(h, p, d_atoms, d_results, d_maps, use_graph);
 }
 
 int tcw_plan_run_timed(tcw_handle *h, tcw_plan *p, const float *d_atoms, tcw_result *d_results,
@@ -922,9 +945,11 @@ int tcw_plan_run_timed(tcw_handle *h, tcw_plan *p, const float *d_atoms, tcw_res
                             h->stream));
   TCW_CUDA(h, launch_repack(p->d_T, p->d_exp_list, p->n_exp, d_atoms, p->d_A8, h->stream));
   TCW_CUDA(h, cudaEventRecord(ev[1], h->stream));
-  TCW_CUDA(h, launch_map(TCW_WINDOW_RECT, plan_launch(h, p, TCW_WINDOW_RECT, d_atoms), h->stream));
+  TCW_CUDA(h, launch_map(TCW_WINDOW_RECT, plan_launch(h, p, TCW_WINDOW_RECT, d_atoms, nullptr),
+                         h->stream));
   TCW_CUDA(h, cudaEventRecord(ev[2], h->stream));
-  TCW_CUDA(h, launch_map(TCW_WINDOW_EXP, plan_launch(h, p, TCW_WINDOW_EXP, d_atoms), h->stream));
+  TCW_CUDA(h, launch_map(TCW_WINDOW_EXP, plan_launch(h, p, TCW_WINDOW_EXP, d_atoms, nullptr),
+                         h->stream));
   TCW_CUDA(h, cudaEventRecord(ev[3], h->stream));
   TCW_CUDA(h, launch_finalize(p->d_T, p->n_templates, p->d_parts, d_results, h->stream));
   TCW_CUDA(h, cudaEventRecord(ev[4], h->stream));

@@ -64,15 +64,11 @@ class pyTransientFstatMap:
         self.tau_ML = transientFstatMap_t.tau_ML
 
     def read_from_file(self, file):
-        """Load a ``t0 tau 2F`` text map (lalpulsar write_transientFstatMap_to_fp format)."""
-        table = np.genfromtxt(file, comments="#")
-        n_t0 = np.unique(table[:, 0]).size
-        n_tau = np.unique(table[:, 1]).size
-        self.F_mn = (0.5 * table[:, 2]).reshape(n_t0, n_tau)
-        k = int(np.argmax(table[:, 2]))
-        self.t0_ML = table[k, 0]
-        self.tau_ML = table[k, 1]
-        self.maxF = 0.5 * table[k, 2]
+        """Load a ``t0 tau 2F`` text map (lalpulsar write_transientFstatMap_to_fp
+        format; parsed natively, semantics of tcw:159-184)."""
+        from .formats import read_map_text
+
+        self.F_mn, self.t0_ML, self.tau_ML, self.maxF = read_map_text(file)
 
     def get_maxF_idx(self):
         """(m, n) of the first maximum of F_mn (row-major order)."""
@@ -102,18 +98,15 @@ class pyTransientFstatMap:
         return self.tau_MP
 
     def write_F_mn_to_file(self, tCWfile, windowRange, header=[]):
-        """Write ``t0 tau 2F`` lines (lalpulsar write_transientFstatMap_to_fp format)."""
-        if isinstance(header, str):
-            header = [header]
-        with open(tCWfile, "w") as fp:
-            for line in header:
-                fp.write("# {:s}\n".format(line))
-            fp.write("# t0[s]     tau[s]     2F\n")
-            for m in range(self.F_mn.shape[0]):
-                t0 = windowRange.t0 + m * windowRange.dt0
-                for n in range(self.F_mn.shape[1]):
-                    tau = windowRange.tau + n * windowRange.dtau
-                    fp.write("  %10d %10d %- 11.8g\n" % (t0, tau, 2.0 * self.F_mn[m, n]))
+        """Write ``t0 tau 2F`` lines (lalpulsar write_transientFstatMap_to_fp
+        format, tcw:289-317), formatted natively."""
+        from .formats import write_map_text
+        from .window import uniform_grid
+
+        N_t0, N_tau = self.F_mn.shape
+        t0s = uniform_grid(int(windowRange.t0), int(windowRange.dt0), N_t0)
+        taus = uniform_grid(int(windowRange.tau), int(windowRange.dtau), N_tau)
+        write_map_text(tCWfile, self.F_mn, t0s, taus, header)
 
 
 # ------------------------------------------------------------------ versions
