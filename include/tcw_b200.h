@@ -152,6 +152,12 @@ int tcw_plan_run_host(tcw_handle *h, tcw_plan *plan, const float *atoms, tcw_res
  * core.py:1534-1540 read cells of full maps). */
 int tcw_plan_run_maps(tcw_handle *h, tcw_plan *plan, const float *d_atoms, tcw_result *d_results,
                       float *d_maps, int use_graph);
+/* Host-buffer form of tcw_plan_run_maps: host atoms in, results and all maps
+ * (tcw_plan_info's n_cells floats) out; synchronises.  A plan created with
+ * TCW_FLAG_POSTERIORS fills t0_mp_idx / tau_mp_idx of every result from the
+ * maps (tcw:219-287); such a plan only runs through the _maps entry points. */
+int tcw_plan_run_maps_host(tcw_handle *h, tcw_plan *plan, const float *atoms, tcw_result *results,
+                           float *maps);
 /* One run without a graph and with the two map kernels one after the other,
  * CUDA events between the kernels on the handle's stream; synchronises and
  * writes the durations (ms) of the prefix, rectangular-map, exponential-map

@@ -97,6 +97,7 @@ SIGNATURES = {
                                      ctypes.POINTER(_c_u64), ctypes.POINTER(TcwTileConfig)]),
     "tcw_plan_run": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int]),
     "tcw_plan_run_maps": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, ctypes.c_int]),
+    "tcw_plan_run_maps_host": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp]),
     "tcw_plan_run_host": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
     "tcw_plan_run_timed": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.POINTER(ctypes.c_float)]),
     "tcw_debug_fail_alloc": (ctypes.c_int, [_vp, ctypes.c_int]),
@@ -376,6 +377,19 @@ class Plan:
         check(load().tcw_plan_run_host(self.handle.ptr, self._p, atoms7.ctypes.data,
                                        res.ctypes.data), self.handle.ptr)
         return res
+
+    def run_maps_host(self, atoms7):
+        """Host atoms in; (results, maps) out, maps a flat float32 array of
+        ``n_cells`` values (template k's map at the sum of the earlier
+        templates' cells)."""
+        atoms7 = np.ascontiguousarray(atoms7, dtype=np.float32)
+        if atoms7.shape[0] < self.n_atom_rows:
+            raise ValueError("atoms array shorter than the plan's atom rows")
+        res = np.zeros(self.n_templates, dtype=RESULT_DTYPE)
+        maps = np.empty(self.n_cells, dtype=np.float32)
+        check(load().tcw_plan_run_maps_host(self.handle.ptr, self._p, atoms7.ctypes.data,
+                                            res.ctypes.data, maps.ctypes.data), self.handle.ptr)
+        return res, maps
 
     def close(self):
         if getattr(self, "_p", None):

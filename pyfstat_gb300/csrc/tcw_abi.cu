@@ -42,6 +42,7 @@ struct tcw_handle {
 struct tcw_plan {
   int device = 0;
   int prec = kPrecFF;
+  int flags = 0;
   uint32_t n_templates = 0, n_items = 0, n_rect = 0;
   uint32_t n_items_rect = 0, n_items_exp = 0, n_blocks_rect = 0, n_blocks_exp = 0;
   uint64_t n_cells = 0, n_atom_rows = 0, p_rows = 0;
@@ -64,6 +65,7 @@ struct tcw_plan {
   // buffers of the host-buffer entry point
   float *d_atoms_in = nullptr;
   tcw_result *d_res_out = nullptr;
+  float *d_maps_out = nullptr;  // maps of tcw_plan_run_maps_host (n_cells floats)
 };
 
 namespace {
@@ -652,8 +654,6 @@ int tcw_plan_create(tcw_handle *h, const tcw_template_desc *desc, uint32_t n_tem
   *out = nullptr;
   if (!desc || n_templates == 0 || !t0s || !taus)
     return set_err(h, TCW_ERR_INVALID_ARG, "empty or null template list / grids");
-  if (flags & TCW_FLAG_POSTERIORS)
-    return set_err(h, TCW_ERR_INVALID_ARG, "batched plans compute no posteriors (no map)");
   int rc = set_device(h);
   if (rc) return rc;
   tcw_tile_config cfg{};
@@ -664,6 +664,7 @@ int tcw_plan_create(tcw_handle *h, const tcw_template_desc *desc, uint32_t n_tem
   if (!p) return TCW_ERR_ALLOC;
   p->device = h->device;
   p->prec = prec_of(flags);
+  p->flags = flags;
   p->n_templates = n_templates;
   p->cfg = cfg;
   std::vector<TemplateDev> T(n_templates);
@@ -816,6 +817,7 @@ int tcw_plan_destroy(tcw_plan *p) {
   if (p->d_buf) cudaFree(p->d_buf);
   if (p->d_atoms_in) cudaFree(p->d_atoms_in);
   if (p->d_res_out) cudaFree(p->d_res_out);
+  if (p->d_maps_out) cudaFree(p->d_maps_out);
   cudaGetLastError();
   delete p;
   return TCW_OK;
@@ -872,6 +874,8 @@ static int plan_enqueue(tcw_handle *h, tcw_plan *p, const float *d_atoms, tcw_re
   TCW_CUDA(h, cudaEventRecord(h->join_ev, h->side_stream));
   TCW_CUDA(h, cudaStreamWaitEvent(h->stream, h->join_ev, 0));
   TCW_CUDA(h, launch_finalize(p->d_T, p->n_templates, p->d_parts, d_results, h->stream));
+  if (d_maps && (p->flags & TCW_FLAG_POSTERIORS))
+    TCW_CUDA(h, launch_plan_posteriors(p->d_T, p->n_templates, d_maps, d_results, h->stream));
   return TCW_OK;
 }
 
@@ -881,6 +885,9 @@ static int plan_run(tcw_handle *h, tcw_plan *p, const float *d_atoms, tcw_result
                     float *d_maps, int use_graph) {
   if (!h || !p) return TCW_ERR_INVALID_ARG;
   if (!d_atoms || !d_results) return set_err(h, TCW_ERR_INVALID_ARG, "null device pointer");
+  if ((p->flags & TCW_FLAG_POSTERIORS) && !d_maps)
+    return set_err(h, TCW_ERR_INVALID_ARG,
+                   "posteriors need the maps: run the plan with tcw_plan_run_maps");
   if (p->device != h->device)
     return set_err(h, TCW_ERR_INVALID_ARG, "plan and handle are on different devices");
   int rc = set_device(h);
@@ -1127,6 +1134,42 @@ int tcw_plan_run_host(tcw_handle *h, tcw_plan *p, const float *atoms, tcw_result
   if (rc) return rc;
   TCW_CUDA(h, cudaMemcpyAsync(results, p->d_res_out, sizeof(tcw_result) * p->n_templates,
                               cudaMemcpyDeviceToHost, h->stream));
+  TCW_CUDA(h, cudaStreamSynchronize(h->stream));
+  return TCW_OK;
+}
+
+int tcw_plan_run_maps_host(tcw_handle *h, tcw_plan *p, const float *atoms, tcw_result *results,
+                           float *maps) {
+  if (!h || !p) return TCW_ERR_INVALID_ARG;
+  if (!atoms || !results || !maps) return set_err(h, TCW_ERR_INVALID_ARG, "null host pointer");
+  int rc = set_device(h);
+  if (rc) return rc;
+  const size_t abytes = sizeof(float) * 7u * (size_t)p->n_atom_rows;
+  const size_t mbytes = sizeof(float) * (size_t)p->n_cells;
+  if (!p->d_atoms_in) {
+    void *a = nullptr, *r = nullptr;
+    rc = ws_alloc(h, &a, std::max<size_t>(abytes, 16));
+    if (rc) return rc;
+    rc = ws_alloc(h, &r, sizeof(tcw_result) * p->n_templates);
+    if (rc) {
+      cudaFree(a);
+      return rc;
+    }
+    p->d_atoms_in = static_cast<float *>(a);
+    p->d_res_out = static_cast<tcw_result *>(r);
+  }
+  if (!p->d_maps_out) {
+    void *m = nullptr;
+    rc = ws_alloc(h, &m, std::max<size_t>(mbytes, 16));
+    if (rc) return rc;
+    p->d_maps_out = static_cast<float *>(m);
+  }
+  TCW_CUDA(h, cudaMemcpyAsync(p->d_atoms_in, atoms, abytes, cudaMemcpyHostToDevice, h->stream));
+  rc = plan_run(h, p, p->d_atoms_in, p->d_res_out, p->d_maps_out, 1);
+  if (rc) return rc;
+  TCW_CUDA(h, cudaMemcpyAsync(results, p->d_res_out, sizeof(tcw_result) * p->n_templates,
+                              cudaMemcpyDeviceToHost, h->stream));
+  TCW_CUDA(h, cudaMemcpyAsync(maps, p->d_maps_out, mbytes, cudaMemcpyDeviceToHost, h->stream));
   TCW_CUDA(h, cudaStreamSynchronize(h->stream));
   return TCW_OK;
 }

@@ -125,6 +125,10 @@ struct DiffLaunch {
 };
 int diff_blocks_per_sm(int pass);
 cudaError_t launch_diff(int pass, const DiffLaunch &L, cudaStream_t stream);
+// Posterior indices of every template of a plan from its written maps.
+cudaError_t launch_plan_posteriors(const TemplateDev *d_T, uint32_t n_templates,
+                                   const float *d_maps, tcw_result *d_results,
+                                   cudaStream_t stream);
 // Full-FP64 direct-summation map of rows rows[0..n_rows) (all rows when rows
 // is NULL) into F[r * N_tau + n]; cond optional.
 cudaError_t launch_map_f64(int window, const float *atoms, const Geom &g, const uint32_t *t0s,

@@ -698,6 +698,101 @@ cudaError_t launch_finalize(const TemplateDev *d_T, uint32_t n_templates, const 
   return cudaGetLastError();
 }
 
+// Batched posteriors of a plan whose maps were written: block k reads
+// template k's map (at map_off) and stores the first-occurrence argmax of
+// the row sums and of the column sums of exp(F - maxF) (tcw:219-287).  Sums
+// in FP32 with Kahan compensation per thread, combined in FP64.
+__global__ void __launch_bounds__(256) plan_posteriors_kernel(const TemplateDev *__restrict__ T,
+                                                              const float *__restrict__ maps,
+                                                              tcw_result *__restrict__ results) {
+  __shared__ double sv[8];
+  __shared__ int64_t si[8];
+  const TemplateDev t = T[blockIdx.x];
+  tcw_result *res = results + blockIdx.x;
+  const float maxF = res->maxF;
+  const float *F = maps + t.map_off;
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  int64_t out_idx[2];
+  for (int pass = 0; pass < 2; pass++) {
+    double best = -1.0;
+    int64_t bidx = INT64_MAX;
+    if (pass == 0) {
+      // rows: one warp per row, lanes over columns
+      for (uint32_t m = warp; m < t.N_t0; m += 8u) {
+        const float *row = F + (size_t)m * t.N_tau;
+        float s = 0.0f, c = 0.0f;
+        for (uint32_t n = lane; n < t.N_tau; n += 32u) {
+          const float y = fsub(exp2f((row[n] - maxF) * kLog2e), c);
+          const float u = fadd(s, y);
+          c = fsub(fsub(u, s), y);
+          s = u;
+        }
+        double v = (double)s - (double)c;
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+        if (v > best) {  // m increases within a warp: keeps the first
+          best = v;
+          bidx = m;
+        }
+      }
+      if (lane != 0) {
+        best = -1.0;
+        bidx = INT64_MAX;
+      }
+    } else {
+      // columns: one thread per column, down all rows
+      for (uint32_t n = threadIdx.x; n < t.N_tau; n += 256u) {
+        float s = 0.0f, c = 0.0f;
+        for (uint32_t m = 0; m < t.N_t0; m++) {
+          const float y = fsub(exp2f((F[(size_t)m * t.N_tau + n] - maxF) * kLog2e), c);
+          const float u = fadd(s, y);
+          c = fsub(fsub(u, s), y);
+          s = u;
+        }
+        const double v = (double)s - (double)c;
+        if (v > best) {
+          best = v;
+          bidx = n;
+        }
+      }
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+      const double ob = __shfl_xor_sync(0xffffffffu, best, d);
+      const int64_t oi = __shfl_xor_sync(0xffffffffu, bidx, d);
+      if (ob > best || (ob == best && oi < bidx)) {
+        best = ob;
+        bidx = oi;
+      }
+    }
+    if (lane == 0) {
+      sv[warp] = best;
+      si[warp] = bidx;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int w = 1; w < 8; w++)
+        if (sv[w] > best || (sv[w] == best && si[w] < bidx)) {
+          best = sv[w];
+          bidx = si[w];
+        }
+      out_idx[pass] = bidx == INT64_MAX ? -1 : bidx;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    res->t0_mp_idx = out_idx[0];
+    res->tau_mp_idx = out_idx[1];
+  }
+}
+
+cudaError_t launch_plan_posteriors(const TemplateDev *d_T, uint32_t n_templates,
+                                   const float *d_maps, tcw_result *d_results,
+                                   cudaStream_t stream) {
+  plan_posteriors_kernel<<<n_templates, 256, 0, stream>>>(d_T, d_maps, d_results);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_posteriors(const TemplateDev *d_T, const float *d_Fmn, void *d_result,
                               double *d_rowsum, double *d_colsum, uint32_t N_t0,
                               uint32_t N_tau, cudaStream_t stream) {
