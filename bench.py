@@ -31,10 +31,6 @@ sys.path.insert(0, REPO)
 METRIC = ("2F-map cells/s, batched+fused vs plain per-template kernel, "
           "2F rel err ≤1e-5")
 UNIT = "cells/s"
-# Algorithmic per-cell work of the transient map (reference per-cell math,
-# compensation not counted): FP32 flops (an FMA counts 2) and MUFU ops.
-FLOPS_PER_CELL = {1: 34.0, 2: 55.0}
-MUFU_PER_CELL = 3.0
 # ncu summaries of the map kernels on this workload; each holds a line
 # "traffic_bytes_per_launch = N" (DRAM read + write bytes of one launch)
 TRAFFIC_FILES = {"rect_map_kernel": os.path.join(REPO, "profiles", "rect_map_kernel_batched.md"),
@@ -168,6 +164,19 @@ def cpu_baseline(templates, seconds, threads):
     return cells / dt, cells, used, dt
 
 
+def cpu_model():
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith(("model name", "cpu part")):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+
+    return platform.processor() or platform.machine()
+
+
 def traffic_per_launch(kernel):
     """DRAM bytes per launch of a map kernel from its committed ncu summary, if any."""
     try:
@@ -184,6 +193,78 @@ def launches_per_step(n_rect, n_exp):
     """Kernels one plan step launches: prefix (rect templates), repack and
     map (exp templates), map (rect templates), finalize."""
     return (2 if n_rect else 0) + (2 if n_exp else 0) + 1
+
+
+# Algorithmic per-cell demand of the fused batched map (the reference's
+# per-cell math; compensation not counted): FP32 flops (an FMA counts 2),
+# MUFU ops (sqrt, rcp, ex2), FP64 flops (D = AB - C^2 and the lnBtSG
+# accumulation).
+DEMAND = {1: {"fp32": 34.0, "mufu": 3.0, "fp64": 3.0},
+          2: {"fp32": 55.0, "mufu": 3.0, "fp64": 3.0}}
+KERNEL_WINDOW = {"rect_map_kernel": 1, "exp_map_kernel": 2}
+
+
+def profile_figure(kernel, key):
+    """A "key = value" figure from the kernel's committed ncu summary."""
+    try:
+        with open(TRAFFIC_FILES[kernel]) as f:
+            for line in f:
+                if line.strip().startswith(key):
+                    return float(line.split("=")[1].split()[0])
+    except (OSError, ValueError, IndexError, KeyError):
+        pass
+    return None
+
+
+def roofline_block(batch, rect_ms, exp_ms, prefix_ms, fin_ms, peaks, clk, n_sms):
+    """Roofline of the dominant map kernel: cells/s against the minimum over
+    {FP32, MUFU, FP64, HBM} of measured peak / per-cell algorithmic demand;
+    with the FP32-flop view and the instruction-issue view of the same kernel."""
+    hbm = None
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            hbm = json.load(f).get("hbm_gbs")
+    except (OSError, ValueError):
+        pass
+    desc = batch.desc
+    kernels = {}
+    for name, w in KERNEL_WINDOW.items():
+        sel = desc["window"] == w
+        cells = float(np.sum(desc["N_t0"][sel].astype(np.float64) * desc["N_tau"][sel]))
+        ms = rect_ms if w == 1 else exp_ms
+        if cells == 0 or ms <= 0:
+            continue
+        # bytes read per launch: the template's atoms once (28 B per atom) + results
+        nbytes = 28.0 * float(np.sum(desc["numAtoms"][sel])) + 40.0 * float(np.sum(sel))
+        d = DEMAND[w]
+        bounds = {"fp32": peaks["fp32_tflops"] * 1e12 / d["fp32"],
+                  "mufu": peaks["mufu_tops"] * 1e12 / d["mufu"],
+                  "fp64": peaks["fp64_tflops"] * 1e12 / d["fp64"]}
+        if hbm:
+            bounds["hbm"] = hbm * 1e9 / (nbytes / cells)
+        bound = min(bounds, key=bounds.get)
+        cps = cells / (ms * 1e-3)
+        k = {"ms": ms, "cells": cells, "cells_per_s": cps, "bound": bound,
+             "roofline_cells_per_s": bounds[bound], "frac": cps / bounds[bound],
+             "unit_bounds_cells_per_s": bounds, "algorithmic_per_cell": d,
+             "algorithmic_bytes_per_launch": nbytes,
+             "fp32_view": {"achieved_tflops": cps * d["fp32"] / 1e12,
+                           "peak_tflops": peaks["fp32_tflops"],
+                           "frac": cps * d["fp32"] / 1e12 / peaks["fp32_tflops"]}}
+        ipc = profile_figure(name, "warp_instructions_per_cell")
+        if ipc and clk and clk.get("sm_mhz"):
+            issue = 4.0 * n_sms * clk["sm_mhz"] * 1e6 / ipc
+            k["issue_view"] = {"warp_instructions_per_cell": ipc,
+                               "issue_bound_cells_per_s": issue, "frac": cps / issue}
+        kernels[name] = k
+    dom = max(kernels, key=lambda n: kernels[n]["ms"])
+    d = kernels[dom]
+    return {"bound": d["bound"], "achieved": d["cells_per_s"], "peak": d["roofline_cells_per_s"],
+            "unit": "cells/s", "frac": d["frac"], "traffic": traffic_per_launch(dom),
+            "kernel": dom, "kernels": kernels, "prefix_ms": prefix_ms, "finalize_ms": fin_ms,
+            "peak_source": "FP32/FP64/MUFU of measured (tcw_probe_peaks on this GPU), HBM of "
+                           "measured (MEASURED_PEAKS.json)",
+            "measured_peaks": dict(peaks, hbm_gbs=hbm)}
 
 
 # ------------------------------------------------------------------ arms
@@ -341,58 +422,22 @@ def run_ours(args, ws, rank, local):
         return
 
     peaks = _lib.probe_peaks(dev.index)
+    roofline = roofline_block(batch, rect_ms, exp_ms, prefix_ms, fin_ms, peaks, clk,
+                              torch.cuda.get_device_properties(dev).multi_processor_count)
     n_rect = int(np.sum(batch.desc["window"] == 1))
-    cells_w = {w: float(np.sum(batch.desc["N_t0"][batch.desc["window"] == w].astype(np.float64)
-                               * batch.desc["N_tau"][batch.desc["window"] == w]))
-               for w in (1, 2)}
-    # per map kernel: algorithmic FP32 flops and MUFU ops per second vs the
-    # measured peaks; the dominant (longest) kernel is the headline roofline
-    per_kernel = {}
-    for w, name, kms_w in ((1, "rect_map_kernel", rect_ms), (2, "exp_map_kernel", exp_ms)):
-        if cells_w[w] == 0 or kms_w <= 0:
-            continue
-        tf = cells_w[w] * FLOPS_PER_CELL[w] / (kms_w * 1e-3) / 1e12
-        mu = cells_w[w] * MUFU_PER_CELL / (kms_w * 1e-3) / 1e12
-        per_kernel[name] = {"ms": kms_w, "cells": cells_w[w],
-                            "cells_per_s": cells_w[w] / (kms_w * 1e-3),
-                            "fp32_tflops": tf, "fp32_frac": tf / peaks["fp32_tflops"],
-                            "mufu_tops": mu, "mufu_frac": mu / peaks["mufu_tops"]}
-    dom = max(per_kernel, key=lambda k: per_kernel[k]["ms"])
-    d = per_kernel[dom]
-    bound = "fp32" if d["fp32_frac"] >= d["mufu_frac"] else "mufu"
-    map_ms = rect_ms + exp_ms
-    roofline = {
-        "bound": bound,
-        "achieved": d["fp32_tflops"] if bound == "fp32" else d["mufu_tops"],
-        "peak": peaks["fp32_tflops"] if bound == "fp32" else peaks["mufu_tops"],
-        "unit": "TFLOP/s" if bound == "fp32" else "Tops/s",
-        "frac": d["fp32_frac"] if bound == "fp32" else d["mufu_frac"],
-        "traffic": traffic_per_launch(dom),
-        "kernel": dom,
-        "kernels": per_kernel, "prefix_ms": prefix_ms, "finalize_ms": fin_ms,
-        "peak_source": "measured on this GPU by tcw_probe_peaks (FMA chains / ex2 chains), "
-                       "of measured",
-        "algorithmic": {"fp32_flops_per_cell": FLOPS_PER_CELL, "mufu_per_cell": MUFU_PER_CELL},
-        "measured_peaks": peaks,
-    }
     atoms_bytes = batch.atoms.nbytes
-    hbm_peak = None
-    try:
-        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
-            hbm_peak = json.load(f).get("hbm_gbs")
-    except (OSError, ValueError):
-        pass
-    roofline["hbm_view"] = {"algorithmic_bytes_per_launch": atoms_bytes + 40 * n_t,
-                            "achieved_gbs": (atoms_bytes + 40 * n_t) / (map_ms * 1e-3) / 1e9,
-                            "peak_gbs": hbm_peak}
 
     cpu = None
     if not args.no_cpu_baseline and ws == 1:
         threads = os.cpu_count() or 1
         v, cells, used, dt = cpu_baseline(templates, args.cpu_seconds, threads)
+        v1, cells1, used1, dt1 = cpu_baseline(templates, args.cpu_seconds / 3.0, 1)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"first {used} templates ({cells} cells, {dt:.1f} s), oracle port of "
-                         "the reference pycuda kernels' FP32 arithmetic + numpy reductions"}
+                         "the reference pycuda kernels' FP32 arithmetic + numpy reductions",
+               "value_1thread": v1,
+               "sample_1thread": f"first {used1} templates ({cells1} cells, {dt1:.1f} s)",
+               "cpu": cpu_model()}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,

@@ -37,8 +37,8 @@ extern "C" {
 // Rectangular window on a uniform windowRange grid.  The reference kernel
 // guards rows with `m < N_tauRange` (Rect.cu:48), so a grid with more t0 rows
 // than tau columns would leave rows unwritten; the harness therefore runs one
-// row per call with win_t0 shifted to that row and the output pointer offset,
-// exactly as the survey of the reference describes.
+// row per call with win_t0 shifted to that row and the output pointer offset
+// by m * N_tau, which is the map the kernel would give without the guard.
 int ref_rect_uniform(float *atoms7, unsigned numAtoms, unsigned TAtom,
                      unsigned t0_data, unsigned win_t0, unsigned win_dt0,
                      unsigned win_tau, unsigned win_dtau, unsigned N_t0,

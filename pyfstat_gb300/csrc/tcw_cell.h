@@ -317,13 +317,29 @@ TCW_HD uint32_t exp_lo(uint32_t t0, const Geom &g) {
   return a > first ? a : first;
 }
 
-// Upper end; false if no atom has t_i <= t1.
+// Upper end; false if no atom has t_i <= t1.  With d = t1 - t0_data >= 0,
+// last = floor(d / TAtom) is the last i with t_i <= t1, and idx_end's
+// unclamped quotient floor((d + TAtom/2) / TAtom) - 1 is last - 1 plus one
+// when the remainder d - last*TAtom reaches TAtom - TAtom/2; the u32 sum
+// d + TAtom/2 wraps only for d > 2^32 - 1 - TAtom/2, left to idx_end.
 TCW_HD bool exp_hi(uint32_t t0, uint32_t tau, const Geom &g, uint32_t &hi) {
   const uint32_t t1 = t0 + 3u * tau;
   if (t1 < g.t0_data) return false;
-  const uint32_t b = idx_end(t1, g);
-  const uint32_t last = fdiv(t1 - g.t0_data, g.div);  // last i with t_i <= t1
-  hi = b < last ? b : last;
+  const uint32_t d = t1 - g.t0_data;
+  const uint32_t last = fdiv(d, g.div);
+  if (d > 0xFFFFFFFFu - g.half) {
+    const uint32_t b = idx_end(t1, g);
+    hi = b < last ? b : last;
+    return true;
+  }
+  // floor((d + half) / TAtom) = last + (rem + half >= TAtom): idx_end's
+  // quotient q = that - 1 (u32), cast to int and clamped as in idx_end; q
+  // never exceeds last, so min(idx_end, last) is idx_end.
+  const uint32_t rem = d - last * g.TAtom;
+  const uint32_t q = last + (rem >= g.TAtom - g.half ? 1u : 0u) - 1u;
+  const int32_t i = (int32_t)q;
+  const uint32_t u = i < 0 ? 0u : (uint32_t)i;
+  hi = u < g.numAtoms ? u : g.numAtoms - 1u;
   return true;
 }
 

@@ -170,6 +170,7 @@ struct Red {
   __device__ __forceinline__ void init() {
     mx = -INFINITY;
     bidx = INT64_MAX;
+    brow = 0;
     s = 0.0f;
     c = 0.0f;
   }
@@ -178,6 +179,28 @@ struct Red {
     float t = fadd(s, y);
     c = fsub(fsub(t, s), y);
     s = t;
+  }
+  // Exponential columns visit rows in descending order at a fixed column:
+  // the first occurrence of the max in row-major order is the last row seen
+  // with it, so only that row is kept per cell (row_to_index forms the flat
+  // index once per column).
+  uint32_t brow;
+  __device__ __forceinline__ void add_row_desc(float F, uint32_t m) {
+    if (F != F) return;  // NaN cells are skipped
+    if (F > mx) {
+      const float sc = ex2_approx((mx - F) * kLog2e);
+      s *= sc;
+      c *= sc;
+      mx = F;
+      brow = m;
+      add_term(1.0f);
+    } else {
+      if (F == mx) brow = m;
+      add_term(ex2_approx((F - mx) * kLog2e));
+    }
+  }
+  __device__ __forceinline__ void row_to_index(uint32_t N_tau, uint32_t n) {
+    if (mx != -INFINITY) bidx = (int64_t)brow * N_tau + n;
   }
   __device__ __forceinline__ void add(float F, int64_t idx) {
     if (F != F) return;  // NaN cells are skipped
@@ -350,9 +373,8 @@ struct MapSink {
   uint32_t N_tau, n;
   Red *red;
   __device__ __forceinline__ void operator()(uint32_t m, float F, bool) {
-    const int64_t idx = (int64_t)m * N_tau + n;
-    if (kWrite) Fmn[idx] = F;
-    red->add(F, idx);
+    if (kWrite) Fmn[(size_t)m * N_tau + n] = F;
+    red->add_row_desc(F, m);
   }
 };
 
@@ -391,6 +413,7 @@ __device__ void exp_tile(const TemplateDev &t, const WorkItem &w, const float *_
       exp_column2<true>(atoms8 + t.a8_off * 8u, t.g, t0s, mb, me, tau, sink, tab);
     else
       exp_column2<false>(atoms8 + t.a8_off * 8u, t.g, t0s, mb, me, tau, sink, tab);
+    red.row_to_index(t.N_tau, n);
   }
 }
 

@@ -65,7 +65,7 @@ def multi_detector_atoms(seed, nsft, ndet=1, Tsft=TSFT_DEFAULT, T0=T0_DEFAULT, a
                          inject=INJECT_RANGE, gap_frac=0.0):
     """A :class:`MultiFstatAtomVector` of ``ndet`` detectors.
 
-    A single detector uses ``default_rng(seed)`` (the config-0 generator);
+    A single detector uses ``default_rng(seed)`` (the single-template 480-SFT generator);
     detector X of several uses ``default_rng([seed, X])``.
     """
     vecs = []
@@ -116,7 +116,7 @@ def batched_templates(n_templates=4096, seed=12345, nsft_range=(200, 4000),
                       ndet=1):
     """Batched workload: per-template SFT count, gap fraction, window and grid.
 
-    Template k uses atoms seed ``seed + k`` (config-0 generator with a random
+    Template k uses atoms seed ``seed + k`` (the single-detector generator with a random
     phase per template); even k rectangular, odd k exponential.  Grids are
     uniform windowRange grids covering the data span:
     ``dt0 = max(1, span // N_t0)``, ``tau = Tsft + n * dtau`` with

@@ -151,7 +151,7 @@ def test_differentiation_workload_256x2000x1024sq(torch_cuda):
     ga, gt = batch.backward_raw(atoms, tmin, tmax, lnB, soft, zero, one)
     torch.cuda.synchronize()
     t2 = time.perf_counter()
-    print(f"\nconfig-3 workload: forward {1e3 * (t1 - t0):.1f} ms, backward "
+    print(f"\n256 templates x 2000 SFTs x 2 detectors, 1024 x 1024: forward {1e3 * (t1 - t0):.1f} ms, backward "
           f"{1e3 * (t2 - t1):.1f} ms for {256 * 1024 * 1024:.3g} cells")
     assert torch.isfinite(ga).all() and torch.isfinite(gt).all()
     for k in (0, 17, 255):
