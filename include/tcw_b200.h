@@ -180,7 +180,7 @@ typedef struct {
   uint32_t t0_data;
   uint32_t N_t0;
   uint32_t N_tau;
-  uint32_t pad;
+  uint32_t window;      /* TCW_WINDOW_EXP (or 0) or TCW_WINDOW_RECT */
   double tau_min;
   double tau_max;
 } tcw_diff_desc;

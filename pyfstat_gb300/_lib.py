@@ -65,7 +65,7 @@ DESC_DTYPE = np.dtype([("atom_offset", "<u8"), ("t0_offset", "<u8"), ("tau_offse
                        ("window", "<i4"), ("N_t0", "<u4"), ("N_tau", "<u4")])
 DIFF_DESC_DTYPE = np.dtype([("atom_offset", "<u8"), ("t0_offset", "<u8"), ("numAtoms", "<u4"),
                             ("TAtom", "<u4"), ("t0_data", "<u4"), ("N_t0", "<u4"),
-                            ("N_tau", "<u4"), ("pad", "<u4"), ("tau_min", "<f8"),
+                            ("N_tau", "<u4"), ("window", "<u4"), ("tau_min", "<f8"),
                             ("tau_max", "<f8")])
 assert DIFF_DESC_DTYPE.itemsize == 56
 assert RESULT_DTYPE.itemsize == ctypes.sizeof(TcwResult) == 40

@@ -1,4 +1,4 @@
-"""Differentiable transient statistics of exponential-window maps.
+"""Differentiable transient statistics of exponential- and rectangular-window maps.
 
 For each template, the tau grid is continuous:
 tau_n = tau_min + n (tau_max - tau_min) / (N_tau - 1).  The forward pass
@@ -13,7 +13,8 @@ returns
 the atoms (columns a2, b2, ab, Fa_re, Fa_im, Fb_re, Fb_im) and to tau_min /
 tau_max.  The backward pass recomputes the window sums on the GPU (no map is
 stored).  Window boundaries change in steps with tau and are not
-differentiated; only the window weights are.
+differentiated; only the window weights are -- so rectangular windows, whose
+sums do not depend on tau between boundaries, have zero tau gradients.
 """
 
 import numpy as np
@@ -23,12 +24,13 @@ from . import _lib
 from .window import uniform_grid
 
 
-class ExpDiffBatch:
-    """Geometry of a batch of exponential-window templates for differentiation.
+class DiffBatch:
+    """Geometry of a batch of templates for differentiation.
 
     ``templates``: dicts with ``atoms`` ((numAtoms, 7) float32 binned atoms,
     used for row offsets and as the default input), ``TAtom``, ``t0_data``,
-    ``N_tau``, and a non-decreasing t0 grid (``t0s`` or ``t0, dt0, N_t0``).
+    ``N_tau``, a non-decreasing t0 grid (``t0s`` or ``t0, dt0, N_t0``) and
+    optionally ``window`` (2 exponential, the default; 1 rectangular).
     """
 
     def __init__(self, templates, device=0, temperature=0.1, handle=None):
@@ -42,8 +44,8 @@ class ExpDiffBatch:
                    else uniform_grid(t["t0"], t["dt0"], t["N_t0"]))
             na = int(np.asarray(t["atoms"]).shape[0])
             self.desc[k] = (rows, g0, na, int(t["TAtom"]), int(t["t0_data"]), t0s.shape[0],
-                            int(t["N_tau"]), 0, float(t.get("tau_min", 1.0)),
-                            float(t.get("tau_max", 1.0)))
+                            int(t["N_tau"]), int(t.get("window", _lib.TCW_WINDOW_EXP)),
+                            float(t.get("tau_min", 1.0)), float(t.get("tau_max", 1.0)))
             t0_parts.append(t0s)
             rows += na
             g0 += t0s.shape[0]
@@ -98,6 +100,10 @@ class ExpDiffBatch:
         return ga, gt
 
 
+# the exponential-window name of the same class
+ExpDiffBatch = DiffBatch
+
+
 class _TransientStats(torch.autograd.Function):
     @staticmethod
     def forward(ctx, atoms, tau_min, tau_max, batch):
@@ -127,6 +133,6 @@ def transient_stats(atoms, tau_min, tau_max, batch):
 
     ``atoms``: (rows, 7) CUDA tensor (float32 or float64; computed from its
     float32 values), ``tau_min`` / ``tau_max``: CPU float64 tensors of one
-    value per template, ``batch``: :class:`ExpDiffBatch`.
+    value per template, ``batch``: :class:`DiffBatch`.
     """
     return _TransientStats.apply(atoms, tau_min, tau_max, batch)

@@ -971,16 +971,20 @@ int tcw_plan_run_timed(tcw_handle *h, tcw_plan *p, const float *d_atoms, tcw_res
 // Validates descriptors, uploads descriptors, tiles and grids into the
 // handle's workspace; returns the layout of what follows them.
 struct DiffSetup {
-  size_t o_T, o_items, o_parts, o_t0, o_cnt, o_scratch, total;
+  size_t o_T, o_items, o_parts, o_t0, o_cnt, o_scratch, o_rlist, o_D64, total;
   uint32_t n_items, n_blocks, max_rows;
+  uint32_t n_rect_items, n_rect_blocks, n_rect;
+  uint64_t p_rows;
 };
 
 static int diff_prepare(tcw_handle *h, const tcw_diff_desc *desc, uint32_t n,
                         const uint32_t *t0s, uint64_t n_t0s, int pass, DiffSetup &S) {
   if (!desc || n == 0 || !t0s) return set_err(h, TCW_ERR_INVALID_ARG, "empty template list");
   std::vector<DiffTemplate> T(n);
-  std::vector<DiffItem> items;
+  std::vector<DiffItem> items, ritems;
+  std::vector<uint32_t> rlist;
   uint32_t max_rows = 0;
+  uint64_t p_rows = 0;
   try {
     for (uint32_t k = 0; k < n; k++) {
       const tcw_diff_desc &d = desc[k];
@@ -996,8 +1000,12 @@ static int diff_prepare(tcw_handle *h, const tcw_diff_desc *desc, uint32_t n,
       for (uint32_t m = 1; m < d.N_t0; m++)
         if (g[m] < g[m - 1])
           return set_err(h, TCW_ERR_INVALID_ARG, "template %u: t0 grid must be non-decreasing", k);
-      if ((double)g[d.N_t0 - 1] + 3.0 * d.tau_max >= 4294967295.0)
-        return set_err(h, TCW_ERR_OVERFLOW, "template %u: t0 + 3 tau exceeds the u32 range", k);
+      if (d.window != 0 && d.window != TCW_WINDOW_EXP && d.window != TCW_WINDOW_RECT)
+        return set_err(h, TCW_ERR_INVALID_ARG, "template %u: invalid window type %u", k,
+                       d.window);
+      const bool rect = d.window == TCW_WINDOW_RECT;
+      if ((double)g[d.N_t0 - 1] + (rect ? 1.0 : 3.0) * d.tau_max >= 4294967295.0)
+        return set_err(h, TCW_ERR_OVERFLOW, "template %u: window end exceeds the u32 range", k);
       DiffTemplate t{};
       t.atom_off = d.atom_offset;
       t.t0_off = d.t0_offset;
@@ -1006,38 +1014,62 @@ static int diff_prepare(tcw_handle *h, const tcw_diff_desc *desc, uint32_t n,
       t.N_tau = d.N_tau;
       t.tau_min = d.tau_min;
       t.tau_max = d.tau_max;
-      t.part_off = (uint32_t)items.size();
-      for (uint32_t n0 = 0; n0 < d.N_tau; n0 += 128u)
-        items.push_back(DiffItem{k, (uint32_t)items.size(), n0, std::min(d.N_tau, n0 + 128u)});
-      t.n_parts = (uint32_t)items.size() - t.part_off;
+      t.window = rect ? (uint32_t)TCW_WINDOW_RECT : (uint32_t)TCW_WINDOW_EXP;
+      std::vector<DiffItem> &dst = rect ? ritems : items;
+      t.part_off = (uint32_t)dst.size();  // rect parts are shifted past the exp ones below
+      // exp tiles: 128 tau columns, all rows; rect tiles: 128 t0 rows, all columns
+      const uint32_t extent = rect ? d.N_t0 : d.N_tau;
+      for (uint32_t n0 = 0; n0 < extent; n0 += 128u)
+        dst.push_back(DiffItem{k, (uint32_t)dst.size(), n0, std::min(extent, n0 + 128u)});
+      t.n_parts = (uint32_t)dst.size() - t.part_off;
+      if (rect) {
+        t.p_off = p_rows;
+        p_rows += (uint64_t)d.numAtoms + 1u;
+        rlist.push_back(k);
+      } else {
+        max_rows = std::max(max_rows, d.N_t0);
+      }
       T[k] = t;
-      max_rows = std::max(max_rows, d.N_t0);
     }
+    const uint32_t n_exp_items = (uint32_t)items.size();
+    for (DiffItem &it : ritems) it.part += n_exp_items;
+    for (uint32_t k : rlist) T[k].part_off += n_exp_items;
+    items.insert(items.end(), ritems.begin(), ritems.end());
+    S.n_rect_items = (uint32_t)ritems.size();
+    S.n_items = n_exp_items;
   } catch (const std::bad_alloc &) {
     return set_err(h, TCW_ERR_ALLOC, "host allocation failed");
   }
-  S.n_items = (uint32_t)items.size();
   S.max_rows = max_rows;
+  S.n_rect = (uint32_t)rlist.size();
+  S.p_rows = p_rows;
   S.n_blocks = (uint32_t)std::max<uint64_t>(
       1, std::min<uint64_t>(S.n_items, (uint64_t)diff_blocks_per_sm(pass) * h->n_sms));
+  S.n_rect_blocks = (uint32_t)std::max<uint64_t>(
+      1, std::min<uint64_t>(S.n_rect_items, (uint64_t)rect_diff_blocks_per_sm(pass) * h->n_sms));
+  const size_t n_all_items = (size_t)S.n_items + S.n_rect_items;
   Layout L;
   S.o_T = L.add(sizeof(DiffTemplate) * n);
-  S.o_items = L.add(sizeof(DiffItem) * S.n_items);
+  S.o_items = L.add(sizeof(DiffItem) * n_all_items);
   S.o_t0 = L.add(sizeof(uint32_t) * n_t0s);
-  S.o_cnt = L.add(sizeof(uint32_t));
+  S.o_cnt = L.add(2 * sizeof(uint32_t));
+  S.o_rlist = L.add(sizeof(uint32_t) * std::max<size_t>(1, rlist.size()));
   const size_t ctl = L.total;
-  S.o_parts = L.add(sizeof(DiffPartial) * S.n_items);
-  S.o_scratch =
-      pass == 1 ? L.add(sizeof(float) * TCW_DIFF_SLOTS * 128u * (size_t)max_rows * S.n_blocks) : 0;
+  S.o_parts = L.add(sizeof(DiffPartial) * n_all_items);
+  S.o_scratch = (pass == 1 && S.n_items)
+                    ? L.add(sizeof(float) * TCW_DIFF_SLOTS * 128u * (size_t)max_rows * S.n_blocks)
+                    : 0;
+  S.o_D64 = pass == 1 ? L.add(sizeof(double) * 8u * std::max<uint64_t>(1, p_rows)) : 0;
   S.total = L.total;
   int rc = ensure_ws(h, S.total);
   if (rc) return rc;
   rc = ensure_stage(h, ctl);
   if (rc) return rc;
   memcpy(h->h_stage + S.o_T, T.data(), sizeof(DiffTemplate) * n);
-  memcpy(h->h_stage + S.o_items, items.data(), sizeof(DiffItem) * S.n_items);
+  memcpy(h->h_stage + S.o_items, items.data(), sizeof(DiffItem) * n_all_items);
   memcpy(h->h_stage + S.o_t0, t0s, sizeof(uint32_t) * n_t0s);
-  memset(h->h_stage + S.o_cnt, 0, sizeof(uint32_t));
+  memset(h->h_stage + S.o_cnt, 0, 2 * sizeof(uint32_t));
+  if (!rlist.empty()) memcpy(h->h_stage + S.o_rlist, rlist.data(), sizeof(uint32_t) * rlist.size());
   TCW_CUDA(h, cudaMemcpyAsync(h->d_ws, h->h_stage, ctl, cudaMemcpyHostToDevice, h->stream));
   TCW_CUDA(h, cudaEventRecord(h->stage_ev, h->stream));
   h->stage_pending = true;
@@ -1056,6 +1088,13 @@ static DiffLaunch diff_launch(tcw_handle *h, const DiffSetup &S, const float *d_
   L.t0s = reinterpret_cast<const uint32_t *>(h->d_ws + S.o_t0);
   L.temp = temperature;
   L.parts = reinterpret_cast<DiffPartial *>(h->d_ws + S.o_parts);
+  L.rect_items = L.items + S.n_items;
+  L.n_rect_items = S.n_rect_items;
+  L.n_rect_blocks = S.n_rect_blocks;
+  L.rect_counter = L.counter + 1;
+  L.rect_list = reinterpret_cast<const uint32_t *>(h->d_ws + S.o_rlist);
+  L.n_rect = S.n_rect;
+  L.D64 = S.o_D64 ? reinterpret_cast<double *>(h->d_ws + S.o_D64) : nullptr;
   return L;
 }
 
@@ -1107,6 +1146,8 @@ int tcw_expdiff_backward(tcw_handle *h, const tcw_diff_desc *desc, uint32_t n_te
   L.grad_tau = d_grad_tau;
   TCW_CUDA(h, cudaMemsetAsync(d_grad_atoms, 0, sizeof(double) * 7u * n_atom_rows, h->stream));
   TCW_CUDA(h, cudaMemsetAsync(d_grad_tau, 0, sizeof(double) * 2u * n_templates, h->stream));
+  if (S.n_rect)
+    TCW_CUDA(h, cudaMemsetAsync(L.D64, 0, sizeof(double) * 8u * S.p_rows, h->stream));
   TCW_CUDA(h, launch_diff(1, L, h->stream));
   return TCW_OK;
 }

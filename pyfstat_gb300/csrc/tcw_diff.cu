@@ -1,4 +1,5 @@
-// Differentiable exponential-window maps: forward values and the adjoint.
+// Differentiable transient maps (exponential and rectangular windows):
+// forward values and the adjoint.
 //
 // Per template the tau grid is continuous, tau_n = tau_min + n (tau_max -
 // tau_min) / (N_tau - 1), and the outputs are
@@ -25,6 +26,15 @@
 //            are reduced across the block and added to the atom gradient.
 // The window-sum factor e^(-k (t_lo - t0)/tau) is left out everywhere: F does
 // not depend on it, so neither do g, dF/dW (in this frame) or dF/dtau.
+//
+// Rectangular windows (rect_diff_kernel): one thread per t0 row, the tau
+// columns in ascending order with FP64 running sums (the window end only
+// grows with tau, as in the reference's running sums, Rect.cu:75-91); the
+// sums of a window do not depend on tau between boundaries, so dL/dtau = 0.
+// The atom gradient is scattered as a difference array: +sum_n G(m, n) at
+// the row's start index lo(m), -G(m, n) at end(m, n) + 1 (consecutive cells
+// with the same end merged), then one prefix scan per template
+// (rect_diff_scan_kernel) gives dL/dx(i) = sum_{j <= i} D(j).
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -376,6 +386,175 @@ __global__ void __launch_bounds__(kDiffBlock)
   }
 }
 
+
+// ------------------------------------------------------------ rectangular windows
+
+// Inclusive end index of a rectangular window for a real tau (the
+// reference's i_t1, Rect.cu:54-69, with t1 = t0 + tau real); t0 >= t0_data -
+// TAtom/2 (checked on the host), so the quotient is >= -1.
+__device__ __forceinline__ uint32_t rect_end_real(uint32_t t0, double tau, const Geom &g) {
+  const double d = (double)t0 + tau - (double)g.t0_data + (double)g.half;
+  const double q = floor(d / (double)g.TAtom) - 1.0;
+  return q < 0.0 ? 0u : (q >= (double)(g.numAtoms - 1u) ? g.numAtoms - 1u : (uint32_t)q);
+}
+
+__device__ __forceinline__ void flush_diff(double *D, uint32_t row, const double v[7], double sgn) {
+#pragma unroll
+  for (int c = 0; c < 7; c++)
+    if (v[c] != 0.0) atomicAdd(D + (size_t)row * 8u + c, sgn * v[c]);
+}
+
+template <int kPass>
+__global__ void __launch_bounds__(kDiffBlock)
+    rect_diff_kernel(const DiffTemplate *__restrict__ T, const DiffItem *__restrict__ items,
+                     uint32_t n_items, uint32_t *__restrict__ counter,
+                     const float *__restrict__ atoms, const uint32_t *__restrict__ t0s_all,
+                     double temp, DiffPartial *__restrict__ parts,
+                     const double *__restrict__ lnZ1, const double *__restrict__ lnZ2,
+                     const double *__restrict__ gB, const double *__restrict__ gS,
+                     double *__restrict__ D64) {
+  __shared__ uint32_t s_item;
+  __shared__ double sh[kDiffBlock / 32][4];
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(counter, 1u);
+    __syncthreads();
+    const uint32_t it = s_item;
+    __syncthreads();
+    if (it >= n_items) break;
+    const DiffItem w = items[it];
+    const DiffTemplate t = T[w.tmpl];
+    const uint32_t m = w.n0 + threadIdx.x;  // this thread's t0 row
+    const bool active = m < w.n1;
+    double m1 = -INFINITY, s1 = 0.0, m2 = -INFINITY, s2 = 0.0;
+    double z1 = 0.0, z2 = 0.0, gb = 0.0, gs = 0.0;
+    if (kPass == 1) {
+      z1 = lnZ1[w.tmpl] - log(70.0 / ((double)t.N_t0 * (double)t.N_tau));
+      z2 = lnZ2[w.tmpl] / temp;
+      gb = gB[w.tmpl];
+      gs = gS[w.tmpl];
+    }
+    if (active) {
+      const float *x = atoms + t.atom_off * 7u;
+      double *D = kPass == 1 ? D64 + t.p_off * 8u : nullptr;
+      const uint32_t t0 = __ldg(t0s_all + t.t0_off + m);
+      const uint32_t lo = idx_start(t0, t.g);
+      double S[7] = {0, 0, 0, 0, 0, 0, 0};
+      double R[7] = {0, 0, 0, 0, 0, 0, 0}, acc[7] = {0, 0, 0, 0, 0, 0, 0};
+      uint32_t next = lo, acc_end = 0xFFFFFFFFu;
+      for (uint32_t n = 0; n < t.N_tau; n++) {
+        const uint32_t end = rect_end_real(t0, tau_of(t, n), t.g);
+        for (; next <= end; next++) {
+#pragma unroll
+          for (int c = 0; c < 7; c++) S[c] += (double)__ldg(x + (size_t)next * 7u + c);
+        }
+        F64Cell fc{2.0, 0.0, false};
+        if (end >= lo) fc = fstat64(S);
+        const double F = fc.F;
+        if (kPass == 0) {
+          lse_add(m1, s1, F);
+          lse_add(m2, s2, 2.0 * F / temp);
+        } else if (fc.ok) {
+          const double g = gb * exp(F - z1) + gs * 2.0 * exp(2.0 * F / temp - z2);
+          const double A = S[0], B = S[1], C = S[2], iD = 1.0 / fc.D;
+          const double Fa2 = S[3] * S[3] + S[4] * S[4], Fb2 = S[5] * S[5] + S[6] * S[6];
+          const double re = S[3] * S[5] + S[4] * S[6];
+          double G[7];
+          G[0] = (Fb2 - F * B) * iD;
+          G[1] = (Fa2 - F * A) * iD;
+          G[2] = (2.0 * F * C - 2.0 * re) * iD;
+          G[3] = 2.0 * (B * S[3] - C * S[5]) * iD;
+          G[4] = 2.0 * (B * S[4] - C * S[6]) * iD;
+          G[5] = 2.0 * (A * S[5] - C * S[3]) * iD;
+          G[6] = 2.0 * (A * S[6] - C * S[4]) * iD;
+          if (end != acc_end) {
+            if (acc_end != 0xFFFFFFFFu) flush_diff(D, acc_end + 1u, acc, -1.0);
+#pragma unroll
+            for (int c = 0; c < 7; c++) acc[c] = 0.0;
+            acc_end = end;
+          }
+#pragma unroll
+          for (int c = 0; c < 7; c++) {
+            acc[c] += g * G[c];
+            R[c] += g * G[c];
+          }
+        }
+      }
+      if (kPass == 1) {
+        if (acc_end != 0xFFFFFFFFu) flush_diff(D, acc_end + 1u, acc, -1.0);
+        flush_diff(D, lo, R, 1.0);
+      }
+    }
+    if (kPass == 0) {
+#pragma unroll
+      for (int d = 16; d > 0; d >>= 1) {
+        const double om1 = __shfl_down_sync(0xffffffffu, m1, d);
+        const double os1 = __shfl_down_sync(0xffffffffu, s1, d);
+        const double om2 = __shfl_down_sync(0xffffffffu, m2, d);
+        const double os2 = __shfl_down_sync(0xffffffffu, s2, d);
+        lse_merge(m1, s1, om1, os1);
+        lse_merge(m2, s2, om2, os2);
+      }
+      if ((threadIdx.x & 31u) == 0) {
+        sh[threadIdx.x >> 5][0] = m1;
+        sh[threadIdx.x >> 5][1] = s1;
+        sh[threadIdx.x >> 5][2] = m2;
+        sh[threadIdx.x >> 5][3] = s2;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        for (int k = 1; k < kDiffBlock / 32; k++) {
+          lse_merge(m1, s1, sh[k][0], sh[k][1]);
+          lse_merge(m2, s2, sh[k][2], sh[k][3]);
+        }
+        parts[w.part] = DiffPartial{m1, s1, m2, s2};
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// dL/dx(i) = sum_{j <= i} D(j) for i < numAtoms, one block per rectangular
+// template: per-thread chunk sums, an exclusive scan of the chunk sums, then
+// each chunk written in order.
+constexpr int kScanBlock = 256;
+
+__global__ void __launch_bounds__(kScanBlock)
+    rect_diff_scan_kernel(const DiffTemplate *__restrict__ T, const uint32_t *__restrict__ list,
+                          const double *__restrict__ D64, double *__restrict__ grad_atoms) {
+  __shared__ double sh[kScanBlock][7];
+  const DiffTemplate t = T[list[blockIdx.x]];
+  const uint32_t n = t.g.numAtoms;
+  const double *D = D64 + t.p_off * 8u;
+  const uint32_t chunk = (n + kScanBlock - 1u) / kScanBlock;
+  const uint32_t a0 = min(n, threadIdx.x * chunk), a1 = min(n, a0 + chunk);
+  double s[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (uint32_t i = a0; i < a1; i++)
+#pragma unroll
+    for (int c = 0; c < 7; c++) s[c] += D[(size_t)i * 8u + c];
+#pragma unroll
+  for (int c = 0; c < 7; c++) sh[threadIdx.x][c] = s[c];
+  __syncthreads();
+  if (threadIdx.x < 7u) {
+    double run = 0.0;
+    for (int k = 0; k < kScanBlock; k++) {
+      const double v = sh[k][threadIdx.x];
+      sh[k][threadIdx.x] = run;
+      run += v;
+    }
+  }
+  __syncthreads();
+  double run[7];
+#pragma unroll
+  for (int c = 0; c < 7; c++) run[c] = sh[threadIdx.x][c];
+  for (uint32_t i = a0; i < a1; i++) {
+#pragma unroll
+    for (int c = 0; c < 7; c++) {
+      run[c] += D[(size_t)i * 8u + c];
+      grad_atoms[(t.atom_off + i) * 7u + c] = run[c];
+    }
+  }
+}
+
 __global__ void diff_finalize_kernel(const DiffTemplate *__restrict__ T, uint32_t n_templates,
                                      const DiffPartial *__restrict__ parts, double temp,
                                      double *__restrict__ lnB, double *__restrict__ soft) {
@@ -406,17 +585,49 @@ int diff_blocks_per_sm(int pass) {
   return n > 0 ? n : 1;
 }
 
+int rect_diff_blocks_per_sm(int pass) {
+  int n = 0;
+  cudaError_t e =
+      pass == 0
+          ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, rect_diff_kernel<0>, kDiffBlock, 0)
+          : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, rect_diff_kernel<1>, kDiffBlock, 0);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    n = 1;
+  }
+  return n > 0 ? n : 1;
+}
+
 cudaError_t launch_diff(int pass, const DiffLaunch &L, cudaStream_t stream) {
-  if (L.n_items == 0) return cudaSuccess;
-  if (pass == 0)
-    diff_kernel<0><<<L.n_blocks, kDiffBlock, 0, stream>>>(
-        L.T, L.items, L.n_items, L.counter, L.atoms, L.t0s, L.temp, L.parts, nullptr, nullptr,
-        nullptr, nullptr, nullptr, 0, nullptr, nullptr);
-  else
-    diff_kernel<1><<<L.n_blocks, kDiffBlock, 0, stream>>>(
-        L.T, L.items, L.n_items, L.counter, L.atoms, L.t0s, L.temp, nullptr, L.lnZ1, L.lnZ2,
-        L.gB, L.gS, L.scratch, L.scratch_rows, L.grad_atoms, L.grad_tau);
-  return cudaGetLastError();
+  if (L.n_items) {
+    if (pass == 0)
+      diff_kernel<0><<<L.n_blocks, kDiffBlock, 0, stream>>>(
+          L.T, L.items, L.n_items, L.counter, L.atoms, L.t0s, L.temp, L.parts, nullptr, nullptr,
+          nullptr, nullptr, nullptr, 0, nullptr, nullptr);
+    else
+      diff_kernel<1><<<L.n_blocks, kDiffBlock, 0, stream>>>(
+          L.T, L.items, L.n_items, L.counter, L.atoms, L.t0s, L.temp, nullptr, L.lnZ1, L.lnZ2,
+          L.gB, L.gS, L.scratch, L.scratch_rows, L.grad_atoms, L.grad_tau);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  if (L.n_rect_items) {
+    if (pass == 0) {
+      rect_diff_kernel<0><<<L.n_rect_blocks, kDiffBlock, 0, stream>>>(
+          L.T, L.rect_items, L.n_rect_items, L.rect_counter, L.atoms, L.t0s, L.temp, L.parts,
+          nullptr, nullptr, nullptr, nullptr, nullptr);
+    } else {
+      rect_diff_kernel<1><<<L.n_rect_blocks, kDiffBlock, 0, stream>>>(
+          L.T, L.rect_items, L.n_rect_items, L.rect_counter, L.atoms, L.t0s, L.temp, nullptr,
+          L.lnZ1, L.lnZ2, L.gB, L.gS, L.D64);
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+      rect_diff_scan_kernel<<<L.n_rect, kScanBlock, 0, stream>>>(L.T, L.rect_list, L.D64,
+                                                                 L.grad_atoms);
+    }
+    return cudaGetLastError();
+  }
+  return cudaSuccess;
 }
 
 cudaError_t launch_diff_finalize(const DiffTemplate *T, uint32_t n_templates,

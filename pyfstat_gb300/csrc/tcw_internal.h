@@ -89,13 +89,17 @@ cudaError_t launch_posteriors(const TemplateDev *d_T, const float *d_Fmn, void *
                               uint32_t N_tau, cudaStream_t stream);
 
 // ---------------------------------------------------------------- differentiable path
-// One exponential template with a continuous tau grid (tcw_diff.cu).
+// One template with a continuous tau grid (tcw_diff.cu); rectangular
+// templates own, in the backward pass, the difference rows of their atom
+// gradient at p_off: (numAtoms + 1) rows of 8 doubles.
 struct DiffTemplate {
   uint64_t atom_off, t0_off;
   Geom g;
   uint32_t N_t0, N_tau;
   double tau_min, tau_max;
   uint32_t part_off, n_parts;
+  uint32_t window, pad;
+  uint64_t p_off;
 };
 // A tile: columns [n0, n1) (at most 128) of one template, all rows.
 struct DiffItem {
@@ -122,7 +126,17 @@ struct DiffLaunch {
   float *scratch;                    // pass B/C: n_blocks x scratch_rows x TCW_DIFF_SLOTS x 128 floats
   uint32_t scratch_rows;
   double *grad_atoms, *grad_tau;     // pass B/C outputs (accumulated; zero them first)
+  // rectangular templates: their tiles (rows [n0, n1) of one template),
+  // counter and persistent blocks, the list of their template indices and
+  // (backward) the difference rows of the atom gradient (zeroed by the caller)
+  const DiffItem *rect_items;
+  uint32_t n_rect_items, n_rect_blocks;
+  uint32_t *rect_counter;
+  const uint32_t *rect_list;
+  uint32_t n_rect;
+  double *D64;
 };
+int rect_diff_blocks_per_sm(int pass);
 int diff_blocks_per_sm(int pass);
 cudaError_t launch_diff(int pass, const DiffLaunch &L, cudaStream_t stream);
 // Posterior indices of every template of a plan from its written maps.

@@ -57,3 +57,14 @@ def test_torch_reference_gradients_match_finite_differences():
     (lp, sp), (lm, sm) = f(x.detach(), c["tau_max"] + ht), f(x.detach(), c["tau_max"] - ht)
     assert (lp - lm) / (2 * ht) == pytest.approx(float(gmax_l), rel=1e-4, abs=1e-12)
     assert (sp - sm) / (2 * ht) == pytest.approx(float(gmax_s), rel=1e-4, abs=1e-12)
+
+
+def test_torch_reference_rect_map_equals_oracle(oracle):
+    c = small_case(seed=12)
+    tau_min, step = 2700.0, 900.0
+    taus = tau_min + step * np.arange(c["N_tau"])
+    F64 = oracle.map_f64(c["atoms"], 1800, c["t0_data"], 1, c["t0s"], taus.astype(np.uint32))
+    x = torch.from_numpy(c["atoms"].astype(np.float64))
+    _, _, F = R.stats(x, 1800, c["t0_data"], c["t0s"], torch.tensor(tau_min),
+                      torch.tensor(tau_min + step * (c["N_tau"] - 1)), c["N_tau"], window=1)
+    np.testing.assert_allclose(F.numpy(), F64, rtol=1e-10, atol=0)
