@@ -174,6 +174,11 @@ struct Red {
     s = 0.0f;
     c = 0.0f;
   }
+  // Adds 2^d (d <= 0, relative to the running max).  Terms below 2^-60 are
+  // dropped: the sum is >= 1, so even 2^22 of them change it by < 2^-38.
+  __device__ __forceinline__ void add_small(float d) {
+    if (d > -60.0f) add_term(ex2_approx(d));
+  }
   __device__ __forceinline__ void add_term(float e) {
     float y = fsub(e, c);
     float t = fadd(s, y);
@@ -184,7 +189,7 @@ struct Red {
   // the first occurrence of the max in row-major order is the last row seen
   // with it, so only that row is kept per cell (row_to_index forms the flat
   // index once per column).
-  uint32_t brow;
+  uint32_t brow;  // row (exp columns) or column (rect rows) of the max
   __device__ __forceinline__ void add_row_desc(float F, uint32_t m) {
     if (F != F) return;  // NaN cells are skipped
     if (F > mx) {
@@ -196,25 +201,31 @@ struct Red {
       add_term(1.0f);
     } else {
       if (F == mx) brow = m;
-      add_term(ex2_approx((F - mx) * kLog2e));
+      add_small((F - mx) * kLog2e);
     }
   }
   __device__ __forceinline__ void row_to_index(uint32_t N_tau, uint32_t n) {
     if (mx != -INFINITY) bidx = (int64_t)brow * N_tau + n;
   }
-  __device__ __forceinline__ void add(float F, int64_t idx) {
+  // Rectangular rows visit columns in ascending order at a fixed row: a tie
+  // never replaces the earlier maximum, so only the column of a strictly
+  // larger F is kept (brow holds the column here); col_to_index forms the
+  // flat index once per row.
+  __device__ __forceinline__ void add_col_asc(float F, uint32_t n) {
     if (F != F) return;  // NaN cells are skipped
     if (F > mx) {
       const float sc = ex2_approx((mx - F) * kLog2e);
       s *= sc;
       c *= sc;
       mx = F;
-      bidx = idx;
+      brow = n;
       add_term(1.0f);
     } else {
-      if (F == mx && idx < bidx) bidx = idx;
-      add_term(ex2_approx((F - mx) * kLog2e));
+      add_small((F - mx) * kLog2e);
     }
+  }
+  __device__ __forceinline__ void col_to_index(int64_t rowidx) {
+    if (mx != -INFINITY) bidx = rowidx + brow;
   }
 };
 
@@ -311,46 +322,56 @@ __device__ void rect_tile(const TemplateDev &t, const WorkItem &w,
     uint32_t e = idx_end(t0 + __ldg(taus + n), t.g);
     return (wr && ef > e) ? ef : e;
   };
+  const int64_t rowidx = (int64_t)m * t.N_tau;
   // e < numAtoms always, so prefix row e + 1 exists even for empty windows
   uint32_t e_cur = 0;
-  float cur[16];
+  float cur[16], nxt[16];
   if (row_ok && nb < ne) {
     e_cur = end_of(nb);
     ld_row16(P + (size_t)(e_cur + 1u) * kPrefixStride, cur);
   }
-  const int64_t rowidx = (int64_t)m * t.N_tau;
+  // One cell: F of column n from prefix row `a` (end ea); the next column's
+  // prefix row is loaded into `b` (end eb) while this one is computed.
+  auto cell = [&](uint32_t n, uint32_t cb, const float *a, uint32_t ea, float *b,
+                  uint32_t &eb) {
+    if (row_ok && n + 1u < ne) {
+      eb = end_of(n + 1u);
+      ld_row16(P + (size_t)(eb + 1u) * kPrefixStride, b);
+    }
+    float F = 2.0f;
+    if (row_ok) {
+      if (ea >= j0) {
+        bool ok;
+        if (kPrec == kPrecPlain32) {
+          F = fstat_plain32(fsub(a[0], row0[0]), fsub(a[1], row0[1]), fsub(a[2], row0[2]),
+                            fsub(a[3], row0[3]), fsub(a[4], row0[4]), fsub(a[5], row0[5]),
+                            fsub(a[6], row0[6]), ok);
+        } else {
+          FF2 W[4];
+#pragma unroll
+          for (int k = 0; k < 4; k++) {
+            W[k].h = sub2(F2{a[2 * k], a[2 * k + 1]}, F2{row0[2 * k], row0[2 * k + 1]});
+            W[k].l = sub2(F2{a[8 + 2 * k], a[9 + 2 * k]}, F2{row0[8 + 2 * k], row0[9 + 2 * k]});
+          }
+          F = fstat_tiered2<kPrec == kPrecFF_F64Det>(W, ok);
+        }
+      }
+      red.add_col_asc(F, n);
+    }
+    if (kWrite) smw[lane * 33u + (n - cb)] = F;
+  };
   for (uint32_t cb = nb; cb < ne; cb += 32u) {
     const uint32_t ce = min(ne, cb + 32u);
-    for (uint32_t n = cb; n < ce; n++) {
+    // ping-pong between the two row buffers; `cur` holds column n on entry
+    uint32_t n = cb;
+    for (; n + 1u < ce; n += 2u) {
       uint32_t e_nxt = 0;
-      float nxt[16];
-      if (row_ok && n + 1u < ne) {
-        e_nxt = end_of(n + 1u);
-        ld_row16(P + (size_t)(e_nxt + 1u) * kPrefixStride, nxt);
-      }
-      float F = 2.0f;
-      if (row_ok) {
-        if (e_cur >= j0) {
-          bool ok;
-          if (kPrec == kPrecPlain32) {
-            F = fstat_plain32(fsub(cur[0], row0[0]), fsub(cur[1], row0[1]),
-                              fsub(cur[2], row0[2]), fsub(cur[3], row0[3]),
-                              fsub(cur[4], row0[4]), fsub(cur[5], row0[5]),
-                              fsub(cur[6], row0[6]), ok);
-          } else {
-            FF2 W[4];
-#pragma unroll
-            for (int k = 0; k < 4; k++) {
-              W[k].h = sub2(F2{cur[2 * k], cur[2 * k + 1]}, F2{row0[2 * k], row0[2 * k + 1]});
-              W[k].l = sub2(F2{cur[8 + 2 * k], cur[9 + 2 * k]},
-                            F2{row0[8 + 2 * k], row0[9 + 2 * k]});
-            }
-            F = fstat_tiered2<kPrec == kPrecFF_F64Det>(W, ok);
-          }
-        }
-        red.add(F, rowidx + n);
-      }
-      if (kWrite) smw[lane * 33u + (n - cb)] = F;
+      cell(n, cb, cur, e_cur, nxt, e_nxt);
+      cell(n + 1u, cb, nxt, e_nxt, cur, e_cur);
+    }
+    if (n < ce) {  // odd chunk length: one more cell, then its successor moves to `cur`
+      uint32_t e_nxt = 0;
+      cell(n, cb, cur, e_cur, nxt, e_nxt);
 #pragma unroll
       for (int k = 0; k < 16; k++) cur[k] = nxt[k];
       e_cur = e_nxt;
@@ -365,6 +386,7 @@ __device__ void rect_tile(const TemplateDev &t, const WorkItem &w,
       __syncwarp();
     }
   }
+  if (row_ok) red.col_to_index(rowidx);
 }
 
 template <bool kWrite>
@@ -420,7 +442,7 @@ __device__ void exp_tile(const TemplateDev &t, const WorkItem &w, const float *_
 // Minimum resident blocks per SM requested from the register allocator
 // (build-time tunables; 1 leaves the allocation to ptxas).
 #ifndef TCW_RECT_MIN_BLOCKS
-#define TCW_RECT_MIN_BLOCKS 1
+#define TCW_RECT_MIN_BLOCKS 5
 #endif
 #ifndef TCW_EXP_MIN_BLOCKS
 #define TCW_EXP_MIN_BLOCKS 5
