@@ -52,8 +52,9 @@ def parse():
                    help="templates timed with the plain per-template kernel")
     p.add_argument("--window", choices=["both", "rect", "exp"], default="both",
                    help="restrict the workload to one window type (breakdown runs)")
-    p.add_argument("--tile", type=str, default="",
-                   help="tile config as JSON, 'auto' for the autotuner, empty for defaults")
+    p.add_argument("--tile", type=str, default="auto",
+                   help="tile config as JSON, 'auto' for the autotuner (default), "
+                        "'default' for the library defaults")
     return p.parse_args()
 
 
@@ -322,7 +323,7 @@ def run_ours(args, ws, rank, local):
     tile = None
     if args.tile == "auto":
         tile = "auto"
-    elif args.tile:
+    elif args.tile and args.tile != "default":
         tile = json.loads(args.tile)
     batch = TransientMapBatch(templates, device=dev.index, tile_config=tile)
     h = batch.handle

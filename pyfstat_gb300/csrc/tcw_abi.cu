@@ -856,17 +856,20 @@ static MapLaunch plan_launch(const tcw_handle *h, const tcw_plan *p, int window,
   return ml;
 }
 
-// prefix -> (exp tiles on the main stream at high priority || rect tiles on
-// the side stream) -> finalize.  The exp tiles are the long ones; the rect
-// kernel's blocks fill SMs as exp blocks retire.
+// prefix -> repack -> (exp tiles on the main stream at high priority || rect
+// tiles on the side stream) -> finalize.  The exp tiles are the long ones;
+// the rect kernel's blocks fill SMs as exp blocks retire.
 static int plan_enqueue(tcw_handle *h, tcw_plan *p, const float *d_atoms, tcw_result *d_results,
                         float *d_maps) {
   TCW_CUDA(h, cudaMemsetAsync(p->d_counter, 0, 2 * sizeof(uint32_t), h->stream));
   TCW_CUDA(h, launch_prefix(p->d_T, p->d_rect_list, p->n_rect, d_atoms, p->d_P, p->prec,
                             h->stream));
+  TCW_CUDA(h, launch_repack(p->d_T, p->d_exp_list, p->n_exp, d_atoms, p->d_A8, h->stream));
+  // Both map kernels become ready together: the high-priority exp blocks
+  // fill the GPU first, and the persistent rect blocks take the SMs that exp
+  // blocks leave as the exp tile queue runs dry (its tail).
   TCW_CUDA(h, cudaEventRecord(h->fork_ev, h->stream));
   TCW_CUDA(h, cudaStreamWaitEvent(h->side_stream, h->fork_ev, 0));
-  TCW_CUDA(h, launch_repack(p->d_T, p->d_exp_list, p->n_exp, d_atoms, p->d_A8, h->stream));
   TCW_CUDA(h, launch_map(TCW_WINDOW_EXP, plan_launch(h, p, TCW_WINDOW_EXP, d_atoms, d_maps),
                          h->stream));
   TCW_CUDA(h, launch_map(TCW_WINDOW_RECT, plan_launch(h, p, TCW_WINDOW_RECT, d_atoms, d_maps),
