@@ -163,3 +163,35 @@ def test_autotuned_plan_matches_default_plan(tmp_path, monkeypatch):
     assert again.tile_config == cfg
     for x in (again, tuned, ref):
         x.close()
+
+
+def test_plan_maps_and_posteriors_equal_the_plain_path():
+    """tcw_plan_run_maps: every template's map equals the plain per-template
+    map (rect bit for bit, exp within the chunking rounding), and a
+    TCW_FLAG_POSTERIORS plan's posterior indices equal the plain path's."""
+    from pyfstat_gb300 import _lib
+
+    tl = small_templates(n=16, seed=21)
+    flags = _lib.TCW_FLAG_LNBTSG | _lib.TCW_FLAG_POSTERIORS
+    batch = TransientMapBatch(tl, flags=flags)
+    res, maps = batch.plan.run_maps_host(batch.atoms)
+    off = 0
+    for k, t in enumerate(tl):
+        t0s, taus = template_grids(t)
+        n = t0s.size * taus.size
+        F, rec = batch.handle.map_plain_host(t["atoms"], t["TAtom"], t["t0_data"], t["window"],
+                                             t0s, taus, want_map=True, flags=flags)
+        Fb = maps[off:off + n].reshape(t0s.size, taus.size)
+        if t["window"] == 1:
+            assert np.array_equal(Fb, F)
+        else:
+            # both within ~2e-6 of FP64 (tier-1 bound), so within 4e-6 of each other
+            np.testing.assert_allclose(Fb, F, rtol=4e-6)
+        if t["window"] == 1 or np.array_equal(Fb, F):
+            assert res["t0_mp_idx"][k] == rec["t0_mp_idx"]
+            assert res["tau_mp_idx"][k] == rec["tau_mp_idx"]
+        off += n
+    # a posterior plan needs the maps
+    with pytest.raises(_lib.TcwError):
+        batch.run()
+    batch.close()
