@@ -195,3 +195,38 @@ def test_plan_maps_and_posteriors_equal_the_plain_path():
     with pytest.raises(_lib.TcwError):
         batch.run()
     batch.close()
+
+
+def test_golden_cases_in_one_persistent_launch(oracle, golden):
+    """Every golden case (clamps, u32 wrap, tiny grids, gaps, off-grid steps)
+    as one template of a single batched plan with maps and posteriors: each
+    map against the FP64 oracle, and maxF, argmax, lnBtSG and the posterior
+    indices as for the plain path."""
+    from _helpers import golden_case, golden_cases, index_ok, rel_err
+    from pyfstat_gb300 import _lib
+
+    cases = [golden_case(golden, n) for n in golden_cases(golden)]
+    cases = [c for c in cases if c["window"] in (1, 2)]
+    flags = _lib.TCW_FLAG_LNBTSG | _lib.TCW_FLAG_POSTERIORS
+    batch = TransientMapBatch([dict(c, t0s=c["t0s"], taus=c["taus"]) for c in cases],
+                              flags=flags)
+    res, maps = batch.plan.run_maps_host(batch.atoms)
+    off = 0
+    for k, c in enumerate(cases):
+        n = c["t0s"].size * c["taus"].size
+        F = maps[off:off + n].reshape(c["t0s"].size, c["taus"].size)
+        off += n
+        F64, cond = oracle.map_f64(c["atoms"], c["TAtom"], c["t0_data"], c["window"], c["t0s"],
+                                   c["taus"], with_cond=True)
+        rel, nband = rel_err(F, F64, cond)
+        assert rel.max() < REL_TOL, (c["name"], rel.max())
+        assert float(res["maxF"][k]) == float(F.max()), c["name"]
+        assert int(res["argmax"][k]) == int(np.argmax(F)), c["name"]
+        if nband == 0:
+            assert argmax_ok(res["argmax"][k], F64), c["name"]
+            assert float(res["lnBtSG"][k]) == pytest.approx(oracle.lnBtSG(F64), rel=REL_TOL,
+                                                            abs=1e-6), c["name"]
+            e = np.exp(F64 - F64.max())
+            assert index_ok(res["t0_mp_idx"][k], e.sum(axis=1)), c["name"]
+            assert index_ok(res["tau_mp_idx"][k], e.sum(axis=0)), c["name"]
+    batch.close()
