@@ -9,10 +9,14 @@
 //                    rows per cell; exponential tiles run two backward double-word
 //                    recurrences per tau column.  Every block reduces its cells to
 //                    (max F, first argmax, sum exp(F - max F)).
+//   repack_kernel    exponential templates' atoms into 32-byte rows (one 256-bit
+//                    load per recurrence step)
 //   finalize_kernel  per template, merges the tile partials in a fixed order:
 //                    maxF, argmax, lnBtSG in FP64.
 //   posterior kernels  row / column sums of exp(F - maxF) over a written map and
-//                    their argmax (t0 / tau max-posterior bins).
+//                    their argmax (t0 / tau max-posterior bins): one template
+//                    (plain path) or every template of a plan
+//                    (plan_posteriors_kernel).
 // No tensor cores: nothing on this path is a dense contraction.
 #include <math.h>
 #include <stdint.h>
