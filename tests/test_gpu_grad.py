@@ -245,3 +245,20 @@ def test_rect_and_exp_templates_in_one_batch(torch_cuda):
                 fd = (vals[0] - vals[1]) / 2e-6
                 assert float(ga[row + i, ch]) == pytest.approx(fd, rel=1e-4, abs=1e-6 * scale)
         row += n
+
+
+def test_invalid_window_type_is_a_status_error(torch_cuda):
+    torch = torch_cuda
+    from pyfstat_gb300 import _lib
+    from pyfstat_gb300.autograd import DiffBatch
+
+    t = templates_small()[0]
+    b = DiffBatch([dict(t, window=3)])
+    atoms = torch.from_numpy(b.atoms).to("cuda:0")
+    with pytest.raises(_lib.TcwError):
+        b.forward_raw(atoms, [t["tau_min"]], [t["tau_max"]])
+    # the handle stays usable
+    b.desc["window"] = 2
+    lnB, soft = b.forward_raw(atoms, [t["tau_min"]], [t["tau_max"]])
+    torch.cuda.synchronize()
+    assert np.isfinite(float(lnB[0])) and np.isfinite(float(soft[0]))
