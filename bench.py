@@ -422,6 +422,15 @@ def run_ours(args, ws, rank, local):
             torch.distributed.destroy_process_group()
         return
 
+    # the same plan with the determinant in native FP64 (TCW_FLAG_FP64_DET)
+    p64 = _lib.Plan(h, batch.desc, batch.t0s, batch.taus, batch.tile_config,
+                    _lib.TCW_FLAG_LNBTSG | _lib.TCW_FLAG_FP64_DET)
+    k64 = np.array([p64.run_timed(d_atoms, d_res) for _ in range(max(2, args.steps))])
+    p64.close()
+    _, r64_ms, e64_ms, _ = (float(x) for x in k64[1:].mean(axis=0))
+    fp64_det = {"rect_ms": r64_ms, "exp_ms": e64_ms,
+                "note": "map kernels with D = AB - C^2 in native FP64 instead of the "
+                        "error-free FP32 products of the default path"}
     peaks = _lib.probe_peaks(dev.index)
     roofline = roofline_block(batch, rect_ms, exp_ms, prefix_ms, fin_ms, peaks, clk,
                               torch.cuda.get_device_properties(dev).multi_processor_count)
@@ -456,6 +465,7 @@ def run_ours(args, ws, rank, local):
                 "d2h_bytes_per_step": 40 * n_t,
                 "api": "TransientMapBatch.run (tcw_plan_run_host), pinned host atoms"},
         "plain_per_template": plain,
+        "fp64_determinant_variant": fp64_det,
         "gpu_launches": launches_per_step(n_rect, n_t - n_rect) * args.steps,
         "clocks": clk,
     }

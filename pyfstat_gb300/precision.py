@@ -1,9 +1,10 @@
 """Precision report of transient maps at scale.
 
-For each template, the FP32 map of the library's default path (double-word
-compensated window sums, error-free D, FP64 lnBtSG) and of the uncompensated
-FP32 variant (``TCW_FLAG_UNCOMPENSATED``) are compared cell by cell with the
-full-FP64 direct-summation map of ``tcw_map_f64`` on the same device:
+For each template, the FP32 maps of the library's default path (double-word
+compensated window sums, error-free FP32 D, FP64 lnBtSG), of the same with D
+in native FP64 (``TCW_FLAG_FP64_DET``) and of the uncompensated FP32 variant
+(``TCW_FLAG_UNCOMPENSATED``) are compared cell by cell with the full-FP64
+direct-summation map of ``tcw_map_f64`` on the same device:
 
 * every t0 row for the first ``full_templates`` templates (then max2F, the
   argmax and lnBtSG are compared too), every ``row_stride``-th row plus the
@@ -33,6 +34,11 @@ from .batched import template_grids
 THRESHOLD = 1e4
 BAND = 1e-5
 LEVELS = (1e-7, 1e-6, 1e-5, 1e-4)
+# the library's default (double-word sums, error-free FP32 D), the same with
+# D in native FP64, and plain FP32 throughout
+VARIANTS = (("compensated", _lib.TCW_FLAG_LNBTSG),
+            ("compensated_fp64D", _lib.TCW_FLAG_LNBTSG | _lib.TCW_FLAG_FP64_DET),
+            ("uncompensated", _lib.TCW_FLAG_LNBTSG | _lib.TCW_FLAG_UNCOMPENSATED))
 
 
 def _variant_errors(torch, Fv, F64, band, res_v, full, rows_np, N_t0, N_tau):
@@ -67,7 +73,7 @@ def _variant_errors(torch, Fv, F64, band, res_v, full, rows_np, N_t0, N_tau):
 
 
 def template_report(handle, t, full, row_stride, torch, dev):
-    """Errors of one template's FP32 maps (both variants) against FP64."""
+    """Errors of one template's FP32 maps (all variants) against FP64."""
     t0s, taus = template_grids(t)
     N_t0, N_tau = t0s.shape[0], taus.shape[0]
     A = torch.from_numpy(np.ascontiguousarray(t["atoms"], np.float32)).to(dev)
@@ -75,8 +81,7 @@ def template_report(handle, t, full, row_stride, torch, dev):
     d_tau = torch.from_numpy(taus.view(np.int32)).to(dev)
     maps = {}
     t_map = {}
-    for name, flags in (("compensated", _lib.TCW_FLAG_LNBTSG),
-                        ("uncompensated", _lib.TCW_FLAG_LNBTSG | _lib.TCW_FLAG_UNCOMPENSATED)):
+    for name, flags in VARIANTS:
         F = torch.empty((N_t0, N_tau), dtype=torch.float32, device=dev)
         res = torch.zeros(5, dtype=torch.float64, device=dev)
         torch.cuda.synchronize(dev)
@@ -115,7 +120,7 @@ def template_report(handle, t, full, row_stride, torch, dev):
 def summarise(reports):
     s = {"templates": len(reports), "cells_compared": sum(r["cells_compared"] for r in reports),
          "cells_in_threshold_band": sum(r["cells_in_threshold_band"] for r in reports)}
-    for v in ("compensated", "uncompensated"):
+    for v, _ in VARIANTS:
         s[v] = {"max_rel_2F": max(r[v]["max_rel_2F"] for r in reports),
                 "cells_above": {k: sum(r[v]["cells_above"][k] for r in reports)
                                 for k in reports[0][v]["cells_above"]}}
@@ -139,18 +144,23 @@ def markdown(summary, reports, args):
              "", "| variant | max rel err 2F | cells > 1e-7 | > 1e-6 | > 1e-5 | > 1e-4 | "
              "max2F rel err (full) | argmax ok (full) | lnBtSG abs err (full) |",
              "|---|---|---|---|---|---|---|---|---|"]
-    for v in ("compensated", "uncompensated"):
+    for v, _ in VARIANTS:
         x = summary[v]
         c = x["cells_above"]
         lines.append(f"| {v} | {x['max_rel_2F']:.3e} | {c['1e-07']} | {c['1e-06']} | {c['1e-05']} "
                      f"| {c['0.0001']} | {x.get('max2F_rel_err_max', float('nan')):.3e} | "
                      f"{x.get('argmax_ok', 0)}/{x.get('full_templates', 0)} | "
                      f"{x.get('lnBtSG_abs_err_max', float('nan')):.3e} |")
-    lines += ["", "Per template (max rel err of 2F, compensated / uncompensated):", "",
-              "| k | rows | compensated | uncompensated | FP64 reference s |", "|---|---|---|---|---|"]
+    lines += ["", "Per template (max rel err of 2F per variant; map times of one template):", "",
+              "| k | rows | compensated | compensated, FP64 D | uncompensated | map ms (default / "
+              "FP64 D / uncomp.) | FP64 reference s |", "|---|---|---|---|---|---|---|"]
     for k, r in enumerate(reports):
+        sec = r["seconds"]
         lines.append(f"| {k} | {r['rows']} | {r['compensated']['max_rel_2F']:.3e} | "
-                     f"{r['uncompensated']['max_rel_2F']:.3e} | {r['seconds']['f64_reference']:.2f} |")
+                     f"{r['compensated_fp64D']['max_rel_2F']:.3e} | "
+                     f"{r['uncompensated']['max_rel_2F']:.3e} | "
+                     f"{1e3 * sec['map_compensated']:.1f} / {1e3 * sec['map_compensated_fp64D']:.1f}"
+                     f" / {1e3 * sec['map_uncompensated']:.1f} | {sec['f64_reference']:.2f} |")
     return "\n".join(lines) + "\n"
 
 
@@ -175,9 +185,9 @@ def main(argv=None):
     for k, t in enumerate(synth.precision_templates(args.templates, seed=args.seed)):
         r = template_report(handle, t, k < args.full_templates, args.row_stride, torch, dev)
         reports.append(r)
-        print(f"template {k}: rows {r['rows']} compensated {r['compensated']['max_rel_2F']:.3e} "
-              f"uncompensated {r['uncompensated']['max_rel_2F']:.3e} "
-              f"(FP64 reference {r['seconds']['f64_reference']:.2f} s)", flush=True)
+        print(f"template {k}: rows {r['rows']} " + " ".join(
+            f"{v} {r[v]['max_rel_2F']:.3e}" for v, _ in VARIANTS) +
+              f" (FP64 reference {r['seconds']['f64_reference']:.2f} s)", flush=True)
     summary = summarise(reports)
     print(json.dumps(summary))
     if args.json:
