@@ -198,6 +198,13 @@ int tcw_expdiff_backward(tcw_handle *h, const tcw_diff_desc *desc, uint32_t n_te
                          const double *d_grad_lnBtSG, const double *d_grad_softmax2F,
                          double *d_grad_atoms, uint64_t n_atom_rows, double *d_grad_tau);
 
+/* Device-side index checks of a debug build (compiled with -DTCW_DEBUG_CHECKS:
+ * every index of a map / adjoint / reference kernel load or store is checked
+ * and a failure is counted, never trapped).  Writes the number of failed checks
+ * since the library was loaded; returns TCW_ERR_UNSUPPORTED (count 0) in
+ * builds without the checks.  A debugging utility; no reference counterpart. */
+int tcw_debug_check_failures(uint32_t *count);
+
 /* Full-FP64 map by direct summation over each cell's window (FP64 weights
  * and sums, FP64 F with the reference's conditioning test, no recurrence and
  * no compensation): the GPU reference for precision reports.  Device

@@ -103,6 +103,7 @@ SIGNATURES = {
     "tcw_debug_fail_alloc": (ctypes.c_int, [_vp, ctypes.c_int]),
     "tcw_map_plain_noalloc": (ctypes.c_int, [_vp, _vp, _c_u32, _c_u32, _c_u32, ctypes.c_int, _vp,
                                              _c_u32, _vp, _c_u32, _vp, _vp, ctypes.c_int]),
+    "tcw_debug_check_failures": (ctypes.c_int, [ctypes.POINTER(_c_u32)]),
     "tcw_map_f64": (ctypes.c_int, [_vp, _vp, _c_u32, _c_u32, _c_u32, ctypes.c_int, _vp, _c_u32,
                                    _vp, _c_u32, _vp, _c_u32, _vp, _vp]),
     "tcw_expdiff_forward": (ctypes.c_int, [_vp, _vp, _c_u32, _vp, _vp, _c_u64, ctypes.c_double,
@@ -138,8 +139,8 @@ def load(build_if_missing=True):
     with _lock:
         if _lib is not None:
             return _lib
-        path = _build.LIB_PATH
-        if build_if_missing and not _build.up_to_date():
+        path = os.environ.get("PYFSTAT_GB300_LIB") or _build.LIB_PATH
+        if path == _build.LIB_PATH and build_if_missing and not _build.up_to_date():
             _build.build()
         if not os.path.exists(path):
             raise RuntimeError(f"{path} is missing: build it with pyfstat_gb300.build.build()")

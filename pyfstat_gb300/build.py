@@ -40,17 +40,24 @@ def up_to_date():
     return all(os.path.getmtime(p) <= t for p in _inputs())
 
 
-def build(force=False, verbose=False, extra_flags=()):
-    """Compile the library if any source is newer than it; return its path."""
-    if not force and up_to_date():
-        return LIB_PATH
+def build(force=False, verbose=False, extra_flags=(), lib_path=None, build_dir=None):
+    """Compile the library if any source is newer than it; return its path.
+
+    ``lib_path`` / ``build_dir`` build a variant (e.g. with
+    ``extra_flags=("-DTCW_DEBUG_CHECKS",)``) elsewhere; the default is the
+    in-tree library."""
+    if lib_path is None:
+        if not force and up_to_date():
+            return LIB_PATH
+        lib_path = LIB_PATH
+    build_dir = build_dir or (BUILD_DIR if lib_path == LIB_PATH else lib_path + ".objs")
     nvcc = nvcc_path()
-    os.makedirs(BUILD_DIR, exist_ok=True)
+    os.makedirs(build_dir, exist_ok=True)
     common = [GENCODE, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-O2", *extra_flags]
 
     def compile_one(src):
-        obj = os.path.join(BUILD_DIR, os.path.splitext(src)[0] + ".o")
+        obj = os.path.join(build_dir, os.path.splitext(src)[0] + ".o")
         cmd = [nvcc, *common, "-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:
             print(" ".join(cmd), file=sys.stderr)
@@ -61,13 +68,13 @@ def build(force=False, verbose=False, extra_flags=()):
 
     with ThreadPoolExecutor(len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
-    tmp = LIB_PATH + ".tmp"
+    tmp = lib_path + ".tmp"
     cmd = [nvcc, GENCODE, "-shared", "-o", tmp, *objs, "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB_PATH)
-    return LIB_PATH
+    os.replace(tmp, lib_path)
+    return lib_path
 
 
 if __name__ == "__main__":

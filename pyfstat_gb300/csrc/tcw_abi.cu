@@ -1218,6 +1218,18 @@ int tcw_plan_run_maps_host(tcw_handle *h, tcw_plan *p, const float *atoms, tcw_r
   return TCW_OK;
 }
 
+int tcw_debug_check_failures(uint32_t *count) {
+  if (!count) return TCW_ERR_INVALID_ARG;
+  uint64_t n = (uint64_t)dcheck_failures_kernels() + dcheck_failures_diff() +
+               dcheck_failures_f64() + dcheck_failures_noalloc();
+  *count = (uint32_t)std::min<uint64_t>(n, 0xFFFFFFFFull);
+#if defined(TCW_DEBUG_CHECKS)
+  return TCW_OK;
+#else
+  return TCW_ERR_UNSUPPORTED;
+#endif
+}
+
 int tcw_map_f64(tcw_handle *h, const float *d_atoms, uint32_t numAtoms, uint32_t TAtom,
                 uint32_t t0_data, int window, const uint32_t *d_t0s, uint32_t N_t0,
                 const uint32_t *d_taus, uint32_t N_tau, const uint32_t *rows, uint32_t n_rows,

@@ -32,6 +32,37 @@
 #include <math.h>
 #endif
 
+// Debug builds (-DTCW_DEBUG_CHECKS): every index used for a load or store of
+// the map kernels is checked against its array on the device; a failed check
+// increments a per-file device counter (read back by tcw_debug_check_failures)
+// instead of trapping, so a bad index shows up as a count, not a GPU fault.
+#if defined(__CUDACC__) && defined(TCW_DEBUG_CHECKS)
+static __device__ unsigned int tcw_dcheck_failures;
+#if defined(__CUDA_ARCH__)
+#define TCW_DCHECK(cond)                                  \
+  do {                                                    \
+    if (!(cond)) atomicAdd(&tcw_dcheck_failures, 1u);     \
+  } while (0)
+#else
+#define TCW_DCHECK(cond) \
+  do {                   \
+  } while (0)
+#endif
+// Host side: this file's counter (each translation unit has its own).
+static inline unsigned int tcw_dcheck_read() {
+  unsigned int v = 0;
+  if (cudaMemcpyFromSymbol(&v, tcw_dcheck_failures, sizeof(v)) != cudaSuccess) {
+    cudaGetLastError();
+    return 0xFFFFFFFFu;
+  }
+  return v;
+}
+#else
+#define TCW_DCHECK(cond) \
+  do {                   \
+  } while (0)
+#endif
+
 namespace tcw {
 
 // ------------------------------------------------------------ rounding-exact ops
@@ -731,12 +762,14 @@ TCW_HD void exp_column(const float *__restrict__ atoms, const Geom &g,
     while (jH > top) {
       jH--;
       float x[7];
+      TCW_DCHECK(jH < g.numAtoms);
       load_atom(atoms + (size_t)jH * 7u, x);
       exp_step<kComp>(Ehi, x, k);
     }
     while (jL > lo) {
       jL--;
       float x[7];
+      TCW_DCHECK(jL < g.numAtoms);
       load_atom(atoms + (size_t)jL * 7u, x);
       exp_step<kComp>(Elo, x, k);
       if (x[0] != 0.0f || x[1] != 0.0f) nz = jL;
@@ -884,6 +917,7 @@ TCW_HD void exp_column2(const float *__restrict__ atoms8, const Geom &g,
     while (jH > top) {
       jH--;
       F2 x[4];
+      TCW_DCHECK(jH < g.numAtoms);
       load_row8(atoms8 + (size_t)jH * 8u, x);
 #pragma unroll
       for (int c = 0; c < 4; c++) Ehi[c] = ff2_axpy(x[c], k2.rh[c], k2.nrh[c], k2.rl[c], Ehi[c]);
@@ -891,6 +925,7 @@ TCW_HD void exp_column2(const float *__restrict__ atoms8, const Geom &g,
     while (jL > lo) {
       jL--;
       F2 x[4];
+      TCW_DCHECK(jL < g.numAtoms);
       load_row8(atoms8 + (size_t)jL * 8u, x);
 #pragma unroll
       for (int c = 0; c < 4; c++) Elo[c] = ff2_axpy(x[c], k2.rh[c], k2.nrh[c], k2.rl[c], Elo[c]);

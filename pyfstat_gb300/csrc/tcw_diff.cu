@@ -192,6 +192,7 @@ __global__ void __launch_bounds__(kDiffBlock)
           }
           while (jH > top) {
             jH--;
+            TCW_DCHECK(jH < t.g.numAtoms);
 #pragma unroll
             for (int c = 0; c < 7; c++) {
               const double xv = (double)__ldg(x + (size_t)jH * 7u + c);
@@ -201,6 +202,7 @@ __global__ void __launch_bounds__(kDiffBlock)
           }
           while (jL > lo) {
             jL--;
+            TCW_DCHECK(jL < t.g.numAtoms);
             const float a2 = __ldg(x + (size_t)jL * 7u), b2 = __ldg(x + (size_t)jL * 7u + 1u);
 #pragma unroll
             for (int c = 0; c < 7; c++) {
@@ -259,6 +261,7 @@ __global__ void __launch_bounds__(kDiffBlock)
           lse_add(m1, s1, F);
           lse_add(m2, s2, 2.0 * F / temp);
         } else {
+          TCW_DCHECK(m < scratch_rows);
           float *sc = my_scratch + (size_t)m * kDiffSlots * kDiffBlock + threadIdx.x;
 #pragma unroll
           for (int c = 0; c < 7; c++) sc[(size_t)c * kDiffBlock] = (float)G[c];
@@ -398,7 +401,9 @@ __device__ __forceinline__ uint32_t rect_end_real(uint32_t t0, double tau, const
   return q < 0.0 ? 0u : (q >= (double)(g.numAtoms - 1u) ? g.numAtoms - 1u : (uint32_t)q);
 }
 
-__device__ __forceinline__ void flush_diff(double *D, uint32_t row, const double v[7], double sgn) {
+__device__ __forceinline__ void flush_diff(double *D, uint32_t row, const double v[7], double sgn,
+                                           uint32_t numAtoms) {
+  TCW_DCHECK(row <= numAtoms);
 #pragma unroll
   for (int c = 0; c < 7; c++)
     if (v[c] != 0.0) atomicAdd(D + (size_t)row * 8u + c, sgn * v[c]);
@@ -444,6 +449,7 @@ __global__ void __launch_bounds__(kDiffBlock)
       for (uint32_t n = 0; n < t.N_tau; n++) {
         const uint32_t end = rect_end_real(t0, tau_of(t, n), t.g);
         for (; next <= end; next++) {
+          TCW_DCHECK(next < t.g.numAtoms);
 #pragma unroll
           for (int c = 0; c < 7; c++) S[c] += (double)__ldg(x + (size_t)next * 7u + c);
         }
@@ -467,7 +473,7 @@ __global__ void __launch_bounds__(kDiffBlock)
           G[5] = 2.0 * (A * S[5] - C * S[3]) * iD;
           G[6] = 2.0 * (A * S[6] - C * S[4]) * iD;
           if (end != acc_end) {
-            if (acc_end != 0xFFFFFFFFu) flush_diff(D, acc_end + 1u, acc, -1.0);
+            if (acc_end != 0xFFFFFFFFu) flush_diff(D, acc_end + 1u, acc, -1.0, t.g.numAtoms);
 #pragma unroll
             for (int c = 0; c < 7; c++) acc[c] = 0.0;
             acc_end = end;
@@ -480,8 +486,8 @@ __global__ void __launch_bounds__(kDiffBlock)
         }
       }
       if (kPass == 1) {
-        if (acc_end != 0xFFFFFFFFu) flush_diff(D, acc_end + 1u, acc, -1.0);
-        flush_diff(D, lo, R, 1.0);
+        if (acc_end != 0xFFFFFFFFu) flush_diff(D, acc_end + 1u, acc, -1.0, t.g.numAtoms);
+        flush_diff(D, lo, R, 1.0, t.g.numAtoms);
       }
     }
     if (kPass == 0) {
@@ -639,4 +645,15 @@ cudaError_t launch_diff_finalize(const DiffTemplate *T, uint32_t n_templates,
   return cudaGetLastError();
 }
 
+}  // namespace tcw
+
+namespace tcw {
+// Failed debug checks of this file's kernels (0 unless built with TCW_DEBUG_CHECKS).
+unsigned int dcheck_failures_diff() {
+#if defined(TCW_DEBUG_CHECKS)
+  return tcw_dcheck_read();
+#else
+  return 0;
+#endif
+}
 }  // namespace tcw

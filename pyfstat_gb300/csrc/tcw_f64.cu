@@ -72,6 +72,7 @@ __global__ void __launch_bounds__(kF64Block)
     has = lo <= hi;
   }
   has = has && active;
+  TCW_DCHECK(!has || hi < g.numAtoms);
   if (threadIdx.x == 0) s_hi = 0;
   __syncthreads();
   if (has) atomicMax(&s_hi, hi + 1u);
@@ -141,4 +142,15 @@ cudaError_t launch_map_f64(int window, const float *atoms, const Geom &g, const 
   return cudaSuccess;
 }
 
+}  // namespace tcw
+
+namespace tcw {
+// Failed debug checks of this file's kernels (0 unless built with TCW_DEBUG_CHECKS).
+unsigned int dcheck_failures_f64() {
+#if defined(TCW_DEBUG_CHECKS)
+  return tcw_dcheck_read();
+#else
+  return 0;
+#endif
+}
 }  // namespace tcw

@@ -139,6 +139,11 @@ struct DiffLaunch {
 int rect_diff_blocks_per_sm(int pass);
 int diff_blocks_per_sm(int pass);
 cudaError_t launch_diff(int pass, const DiffLaunch &L, cudaStream_t stream);
+// Failed device-side debug checks per translation unit (TCW_DEBUG_CHECKS).
+unsigned int dcheck_failures_kernels();
+unsigned int dcheck_failures_diff();
+unsigned int dcheck_failures_f64();
+unsigned int dcheck_failures_noalloc();
 // Posterior indices of every template of a plan from its written maps.
 cudaError_t launch_plan_posteriors(const TemplateDev *d_T, uint32_t n_templates,
                                    const float *d_maps, tcw_result *d_results,

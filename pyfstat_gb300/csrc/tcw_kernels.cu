@@ -320,6 +320,7 @@ __device__ void rect_tile(const TemplateDev &t, const WorkItem &w,
     j0 = idx_start(t0, t.g);
     wr = rect_row_wrapped(t0, tau_first, t.g);
     ef = wr ? idx_end(t0 + tau_first, t.g) : 0u;
+    TCW_DCHECK(j0 <= t.g.numAtoms);
     ld_row16(P + (size_t)j0 * kPrefixStride, row0);
   }
   auto end_of = [&](uint32_t n) {
@@ -332,6 +333,7 @@ __device__ void rect_tile(const TemplateDev &t, const WorkItem &w,
   float cur[16], nxt[16];
   if (row_ok && nb < ne) {
     e_cur = end_of(nb);
+    TCW_DCHECK(e_cur + 1u <= t.g.numAtoms);
     ld_row16(P + (size_t)(e_cur + 1u) * kPrefixStride, cur);
   }
   // One cell: F of column n from prefix row `a` (end ea); the next column's
@@ -340,6 +342,7 @@ __device__ void rect_tile(const TemplateDev &t, const WorkItem &w,
                   uint32_t &eb) {
     if (row_ok && n + 1u < ne) {
       eb = end_of(n + 1u);
+      TCW_DCHECK(eb + 1u <= t.g.numAtoms);
       ld_row16(P + (size_t)(eb + 1u) * kPrefixStride, b);
     }
     float F = 2.0f;
@@ -399,6 +402,7 @@ struct MapSink {
   uint32_t N_tau, n;
   Red *red;
   __device__ __forceinline__ void operator()(uint32_t m, float F, bool) {
+    TCW_DCHECK(n < N_tau);
     if (kWrite) Fmn[(size_t)m * N_tau + n] = F;
     red->add_row_desc(F, m);
   }
@@ -860,4 +864,15 @@ cudaError_t launch_posteriors(const TemplateDev *d_T, const float *d_Fmn, void *
   return cudaGetLastError();
 }
 
+}  // namespace tcw
+
+namespace tcw {
+// Failed debug checks of this file's kernels (0 unless built with TCW_DEBUG_CHECKS).
+unsigned int dcheck_failures_kernels() {
+#if defined(TCW_DEBUG_CHECKS)
+  return tcw_dcheck_read();
+#else
+  return 0;
+#endif
+}
 }  // namespace tcw

@@ -213,3 +213,14 @@ extern "C" int tcw_map_plain_noalloc(void *stream, const float *d_atoms, uint32_
     return TCW_ERR_CUDA;
   return TCW_OK;
 }
+
+namespace tcw {
+// Failed debug checks of this file's kernels (0 unless built with TCW_DEBUG_CHECKS).
+unsigned int dcheck_failures_noalloc() {
+#if defined(TCW_DEBUG_CHECKS)
+  return tcw_dcheck_read();
+#else
+  return 0;
+#endif
+}
+}  // namespace tcw

@@ -81,3 +81,13 @@ def test_no_fallback_without_gpu():
         tcw.init_transient_fstat_map_features("b200")
     with pytest.raises(Exception, match="not available"):
         tcw.call_compute_transient_fstat_map("b200", features, None, None)
+
+
+def test_release_build_has_no_device_checks():
+    import ctypes
+
+    from pyfstat_gb300 import _lib
+
+    n = ctypes.c_uint32(7)
+    assert _lib.load().tcw_debug_check_failures(ctypes.byref(n)) == _lib.TCW_ERR_UNSUPPORTED
+    assert n.value == 0
