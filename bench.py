@@ -165,6 +165,64 @@ def cpu_baseline(templates, seconds, threads):
     return cells / dt, cells, used, dt
 
 
+def dropin_per_call(h, reps=20):
+    """Median wall time (ms) of one drop-in call, host arrays in and out: the
+    480 x 480 rectangular single-template map through the PyFstat-facing
+    dispatcher (windowRange, BtSG), and the 480 t0 x 512 log-spaced tau
+    exponential map through the C-ABI host entry (tcw_map_plain_host)."""
+    from pyfstat_gb300 import _lib, synth
+    from pyfstat_gb300 import tcw_fstat_map_funcs as tcw
+    from pyfstat_gb300.window import transientWindowRange_t
+
+    def median_ms(fn):
+        for _ in range(3):
+            fn()
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            fn()
+            ts.append(time.perf_counter() - t0)
+        return 1e3 * statistics.median(ts)
+
+    features, ctx = tcw.init_transient_fstat_map_features("b200")
+    multi = synth.multi_detector_atoms(0, 480, 1)
+    wr = dict(type=1, t0=700000000, t0Band=479 * 1800, dt0=1800, tau=1800, tauBand=479 * 1800,
+              dtau=1800)
+    rect_ms = median_ms(lambda: tcw.call_compute_transient_fstat_map(
+        "b200", features, multi, transientWindowRange_t(**wr), BtSG=True))
+    ctx.detach()
+    c = synth.plain_exp_case()
+    flags = _lib.TCW_FLAG_LNBTSG | _lib.TCW_FLAG_POSTERIORS
+    exp_ms = median_ms(lambda: h.map_plain_host(c["atoms"], c["TAtom"], c["t0_data"], 2,
+                                                c["t0s"], c["taus"], want_map=True, flags=flags))
+    return {"rect_480x480_dispatcher_ms": rect_ms, "exp_480x512log_c_abi_ms": exp_ms,
+            "note": "median of 20 calls, full F map and result back on the host"}
+
+
+def cpu_per_call(threads, reps=3):
+    """The same two single-template maps with the oracle port (the reference
+    kernels' FP32 arithmetic) plus its numpy lnBtSG / posteriors, best of 3."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+    from pyfstat_gb300 import synth
+
+    O.build()
+    out = {}
+    for name, c, fn in (("rect_480x480_ms", synth.plain_rect_case(), O.rect_map_f32),
+                        ("exp_480x512log_ms", synth.plain_exp_case(), O.exp_map_f32)):
+        best = None
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            F = fn(c["atoms"], c["TAtom"], c["t0_data"], c["t0s"], c["taus"], nthreads=threads)
+            O.max_argmax(F)
+            O.lnBtSG(F)
+            O.t0_max_posterior_idx(F)
+            dt = 1e3 * (time.perf_counter() - t0)
+            best = dt if best is None else min(best, dt)
+        out[name] = best
+    return out
+
+
 def cpu_model():
     try:
         with open("/proc/cpuinfo") as f:
@@ -431,6 +489,7 @@ def run_ours(args, ws, rank, local):
     fp64_det = {"rect_ms": r64_ms, "exp_ms": e64_ms,
                 "note": "map kernels with D = AB - C^2 in native FP64 instead of the "
                         "error-free FP32 products of the default path"}
+    per_call = dropin_per_call(h)
     peaks = _lib.probe_peaks(dev.index)
     roofline = roofline_block(batch, rect_ms, exp_ms, prefix_ms, fin_ms, peaks, clk,
                               torch.cuda.get_device_properties(dev).multi_processor_count)
@@ -446,6 +505,7 @@ def run_ours(args, ws, rank, local):
                "sample": f"first {used} templates ({cells} cells, {dt:.1f} s), oracle port of "
                          "the reference pycuda kernels' FP32 arithmetic + numpy reductions",
                "value_1thread": v1,
+               "per_call_ms": cpu_per_call(threads),
                "sample_1thread": f"first {used1} templates ({cells1} cells, {dt1:.1f} s)",
                "cpu": cpu_model()}
 
@@ -466,6 +526,7 @@ def run_ours(args, ws, rank, local):
                 "api": "TransientMapBatch.run (tcw_plan_run_host), pinned host atoms"},
         "plain_per_template": plain,
         "fp64_determinant_variant": fp64_det,
+        "dropin_per_call": per_call,
         "gpu_launches": launches_per_step(n_rect, n_t - n_rect) * args.steps,
         "clocks": clk,
     }
