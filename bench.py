@@ -419,7 +419,14 @@ def run_ours(args, ws, rank, local):
         t = torch.tensor([ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
-    value = n_cells * ws / (ms * 1e-3)
+    # whole-job cells and copied bytes: ranks hold different (seeded) template sets
+    total_cells, total_in, total_out = n_cells, batch.atoms.nbytes, 40 * n_t
+    if ws > 1:
+        t = torch.tensor([float(n_cells), float(total_in), float(total_out)],
+                         dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
+        total_cells, total_in, total_out = (float(v) for v in t.tolist())
+    value = total_cells / (ms * 1e-3)
     res = d_res.cpu().numpy().view(_lib.RESULT_DTYPE)
     assert np.all(np.isfinite(res["lnBtSG"])) and np.all(res["maxF"] > 0)
 
@@ -472,7 +479,7 @@ def run_ours(args, ws, rank, local):
         pcells = sum(int(t["N_t0"]) * int(t["N_tau"]) for t in sub)
         pval = pcells / (p0.elapsed_time(p1) * 1e-3)
         plain = {"value": pval, "unit": UNIT, "templates": len(sub),
-                 "ratio_batched_over_plain": value / ws / pval,
+                 "ratio_batched_over_plain": n_cells / (ms * 1e-3) / pval,
                  "note": "one tcw_map_plain call per template, full F map written"}
 
     if rank != 0:
@@ -521,8 +528,8 @@ def run_ours(args, ws, rank, local):
                    "tile_config": batch.tile_config, "parallelism": f"templates x{ws} ranks"},
         "roofline": roofline,
         "cpu_baseline": cpu,
-        "e2e": {"value": n_cells * ws / e2e_s, "unit": UNIT, "h2d_bytes_per_step": atoms_bytes,
-                "d2h_bytes_per_step": 40 * n_t,
+        "e2e": {"value": total_cells / e2e_s, "unit": UNIT,
+                "h2d_bytes_per_step": int(total_in), "d2h_bytes_per_step": int(total_out),
                 "api": "TransientMapBatch.run (tcw_plan_run_host), pinned host atoms"},
         "plain_per_template": plain,
         "fp64_determinant_variant": fp64_det,
