@@ -95,11 +95,13 @@ __device__ __forceinline__ F64Cell fstat64(const double W[7]) {
 
 // Online log-sum-exp in FP64 (exp in FP64 too: the forward values feed
 // finite-difference checks, where FP32 rounding of the terms would show).
+// Terms below e^-60 of the running maximum are skipped: the sum is >= 1, so
+// even 1e9 of them change it by < 1e-17.
 __device__ __forceinline__ void lse_add(double &m, double &s, double v) {
   if (v > m) {
     s = s * exp(m - v) + 1.0;
     m = v;
-  } else {
+  } else if (v - m > -60.0) {
     s += exp(v - m);
   }
 }
@@ -460,7 +462,11 @@ __global__ void __launch_bounds__(kDiffBlock)
           lse_add(m1, s1, F);
           lse_add(m2, s2, 2.0 * F / temp);
         } else if (fc.ok) {
-          const double g = gb * exp(F - z1) + gs * 2.0 * exp(2.0 * F / temp - z2);
+          // dL/dF of this cell (FP32 exponentials: relative 1e-7 on a gradient
+          // term; cells far below the maxima get exactly 0 and are skipped)
+          const double g = gb * (double)exp2f((float)(F - z1) * kLog2eF) +
+                           gs * 2.0 * (double)exp2f((float)(2.0 * F / temp - z2) * kLog2eF);
+          if (g == 0.0) continue;
           const double A = S[0], B = S[1], C = S[2], iD = 1.0 / fc.D;
           const double Fa2 = S[3] * S[3] + S[4] * S[4], Fb2 = S[5] * S[5] + S[6] * S[6];
           const double re = S[3] * S[5] + S[4] * S[6];
