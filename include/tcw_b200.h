@@ -106,11 +106,14 @@ int tcw_device_count(int *count);
 int tcw_device_info(int device, char *name, size_t name_len, int *cc_major, int *cc_minor,
                     size_t *total_mem);
 
-/* Handle: owns a CUDA stream and a grow-only device workspace on `device`. */
+/* Handle: owns a CUDA stream and a grow-only device workspace on `device`
+ * (the pycuda context of tcw:419-470 and its per-call allocations,
+ * tcw:861-912).  tcw_set_stream takes a caller's cudaStream_t, NULL for the
+ * handle's own stream, or cudaStreamLegacy for the legacy default stream. */
 int tcw_create(tcw_handle **h, int device);
 int tcw_destroy(tcw_handle *h);
 int tcw_get_stream(tcw_handle *h, void **stream);
-int tcw_set_stream(tcw_handle *h, void *stream); /* NULL = the handle's own stream */
+int tcw_set_stream(tcw_handle *h, void *stream);
 int tcw_sync(tcw_handle *h, int timeout_ms);     /* TCW_ERR_TIMEOUT if not done in time */
 
 /* Plain per-template map on device buffers.  d_Fmn may be NULL (no map is
@@ -122,7 +125,10 @@ int tcw_map_plain(tcw_handle *h, const float *d_atoms, uint32_t numAtoms, uint32
                   const uint32_t *d_taus, uint32_t N_tau, float *d_Fmn, tcw_result *d_result,
                   int flags);
 
-/* The same with host buffers: copies in, computes, copies out, synchronises. */
+/* The same with host buffers: copies in, computes, copies out, synchronises
+ * -- one call of pycuda_compute_transient_fstat_map's kernel part
+ * (tcw:837-916, :919-998) with its host reductions (tcw:810-828); window
+ * TCW_WINDOW_NONE is one rectangular cell over all data (tcw:742-749). */
 int tcw_map_plain_host(tcw_handle *h, const float *atoms, uint32_t numAtoms, uint32_t TAtom,
                        uint32_t t0_data, int window, const uint32_t *t0s, uint32_t N_t0,
                        const uint32_t *taus, uint32_t N_tau, float *Fmn, tcw_result *result,
@@ -165,8 +171,9 @@ int tcw_plan_run_maps_host(tcw_handle *h, tcw_plan *plan, const float *atoms, tc
 int tcw_plan_run_timed(tcw_handle *h, tcw_plan *plan, const float *d_atoms, tcw_result *d_results,
                        float *ms);
 
-/* Differentiable exponential-window maps (no counterpart in the reference:
- * an addition for gradient-based searches).  Per template the tau grid is
+/* Differentiable maps, exponential or rectangular windows (desc.window; the
+ * "expdiff" names are historical) -- no counterpart in the reference: an
+ * addition for gradient-based searches.  Per template the tau grid is
  * continuous, tau_n = tau_min + n (tau_max - tau_min) / (N_tau - 1); the
  * t0 grid (host array, seconds) must be non-decreasing and start no earlier
  * than t0_data - TAtom/2.  Outputs per template: lnBtSG (ln(70/(N_t0 N_tau))
