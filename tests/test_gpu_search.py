@@ -70,3 +70,16 @@ def test_semicoherent_per_segment_twoF_matches_fp64_oracle(oracle):
         out["log10BSGL"],
         search.compute_log10BSGL(out["twoF"], out["twoFX"],
                                  Fstar0=search.fstar0_semicoherent(nsegs)), rtol=1e-12)
+
+
+def test_grid_batch_window_none_is_the_full_data_cell():
+    """Window type 'none': every point's map is one rectangular cell over its
+    own data (tcw:742-749), so maxTwoF equals the all-data twoF."""
+    pts = points(n=4, nsft=90)
+    out = search.TransientGridBatch(pts, transientWindowRange_t(type=0), BtSG=True).run()
+    for k, multi in enumerate(pts):
+        m = b200_compute_transient_fstat_map(multi, transientWindowRange_t(type=0), BtSG=True)
+        assert out["maxTwoF"][k] == pytest.approx(2 * float(m.maxF), rel=2e-6)
+        assert out["maxTwoF"][k] == out["twoF"][k]
+        assert (out["t0_ML"][k], out["tau_ML"][k]) == (m.t0_ML, m.tau_ML)
+        assert out["lnBtSG"][k] == pytest.approx(m.lnBtSG, rel=2e-6)
