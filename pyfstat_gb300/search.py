@@ -11,7 +11,8 @@ one more map per detector and reads one cell of each
 (core.py:2000-2019, :2240-2289).
 
 Here all points (and all detectors of all points) of a batch are templates
-of ONE batched plan, run in one persistent launch:
+of one batched plan, run in one persistent launch (or one per chunk of
+points when the maps to be written would exceed a device-memory budget):
 
 * :class:`TransientGridBatch` -- maxTwoF, t0_ML, tau_ML, and with ``BtSG``
   lnBtSG, t0_MP, tau_MP (posteriors from the written maps on the GPU), and
@@ -127,6 +128,20 @@ def _grid_for(windowRange, TAtom, t0_data, numAtoms):
     return wtype, uniform_grid(t0, dt0, N_t0), uniform_grid(tau, dtau, N_tau), r
 
 
+def chunks_by_cells(cells, budget_cells):
+    """Consecutive index ranges [a, b) whose summed cells stay within
+    ``budget_cells`` (a range holds at least one item)."""
+    out, a, acc = [], 0, 0
+    for i, c in enumerate(cells):
+        if i > a and acc + c > budget_cells:
+            out.append((a, i))
+            a, acc = i, 0
+        acc += c
+    if a < len(cells):
+        out.append((a, len(cells)))
+    return out
+
+
 def _device_maps_run(templates, flags, device, tile_config=None, handle=None):
     """Results and device maps (torch) of one batched plan over ``templates``."""
     import torch
@@ -161,11 +176,14 @@ class TransientGridBatch:
     BtSG: also lnBtSG and the t0 / tau max-posterior estimates.
     BSGL: also per-detector 2F at the argmax and log10BSGL.
     detector_names: IFO names for the ``twoF<IFO>atMaxTwoF`` columns.
+    map_budget_bytes: device memory for the maps written per launch (BtSG
+        posteriors, BSGL cells); points are processed in consecutive chunks
+        within it (default 8 GiB).
     """
 
     def __init__(self, points, windowRange, BtSG=False, BSGL=False, detector_names=None,
                  device=0, tile_config=None, Fstar0=15.0, oLGX=None, use_log_correction=True,
-                 bsgl=None, flags=_lib.TCW_FLAG_LNBTSG):
+                 bsgl=None, flags=_lib.TCW_FLAG_LNBTSG, map_budget_bytes=8 << 30):
         self.multis = [_as_multi(p) for p in points]
         self.windowRange = windowRange
         self.BtSG = bool(BtSG)
@@ -176,6 +194,9 @@ class TransientGridBatch:
         self.device = device
         self.tile_config = tile_config
         self.flags = int(flags)
+        # device memory for written maps per launch (posteriors, BSGL cells):
+        # larger searches run as several batched launches
+        self.map_budget_cells = max(1, int(map_budget_bytes) // 4)
         self.bsgl = bsgl or (lambda twoF, twoFX: compute_log10BSGL(
             twoF, twoFX, Fstar0=Fstar0, oLGX=oLGX, use_log_correction=use_log_correction))
 
@@ -201,17 +222,24 @@ class TransientGridBatch:
             full_tmpl.append(dict(atoms=A, TAtom=TA, t0_data=t0d, window=TRANSIENT_RECTANGULAR,
                                   t0s=np.array([t0d], np.uint32),
                                   taus=np.array([A.shape[0] * TA], np.uint32)))
-        # all-data 2F (one cell per point) and the transient maps: one plan
+        # all-data 2F (one cell per point) and the transient maps: one plan per
+        # chunk of points (one chunk unless the written maps would exceed the
+        # memory budget)
         flags = self.flags | (_lib.TCW_FLAG_POSTERIORS if self.BtSG else 0)
-        if self.BtSG:
-            res, _, _ = _device_maps_run(maps_tmpl + full_tmpl, flags, self.device,
-                                         self.tile_config)
-        else:
-            b = TransientMapBatch(maps_tmpl + full_tmpl, device=self.device,
-                                  tile_config=self.tile_config, flags=flags)
-            res = b.run()
-            b.close()
-        rmap, rfull = res[:npts], res[npts:]
+        rmap = np.zeros(npts, dtype=_lib.RESULT_DTYPE)
+        rfull = np.zeros(npts, dtype=_lib.RESULT_DTYPE)
+        cells = [int(g[1].size) * int(g[2].size) + 1 for g in grids]
+        budget = self.map_budget_cells if self.BtSG else float("inf")
+        for a, b in chunks_by_cells(cells, budget):
+            tmpl = maps_tmpl[a:b] + full_tmpl[a:b]
+            if self.BtSG:
+                res, _, _ = _device_maps_run(tmpl, flags, self.device, self.tile_config)
+            else:
+                batch = TransientMapBatch(tmpl, device=self.device, tile_config=self.tile_config,
+                                          flags=flags)
+                res = batch.run()
+                batch.close()
+            rmap[a:b], rfull[a:b] = res[:b - a], res[b - a:]
         out["twoF"] = 2.0 * rfull["maxF"].astype(np.float64)
         maxTwoF = 2.0 * rmap["maxF"].astype(np.float64)
         out["maxTwoF"] = np.where(np.isnan(maxTwoF), 0.0, maxTwoF)
@@ -239,6 +267,8 @@ class TransientGridBatch:
         templates (t0 of the argmax row, taus up to the argmax column) of each
         detector's own binned atoms, so that the rectangular running sums
         along tau are those of the full single-detector map (core.py:1531-1541)."""
+        import torch
+
         tmpl, where = [], []
         for k, multi in enumerate(self.multis):
             w, t0s, taus, _ = grids[k]
@@ -247,14 +277,15 @@ class TransientGridBatch:
                 tmpl.append(dict(atoms=A, TAtom=TA, t0_data=t0d, window=w,
                                  t0s=t0s[ms[k]:ms[k] + 1].copy(), taus=taus[:ns[k] + 1].copy()))
                 where.append((k, x, ns[k]))
-        res, d_maps, offs = _device_maps_run(tmpl, self.flags, self.device, self.tile_config)
-        idx = np.array([offs[j] + n for j, (_, _, n) in enumerate(where)], dtype=np.int64)
-        import torch
-
-        vals = d_maps[torch.from_numpy(idx).to(d_maps.device)].cpu().numpy().astype(np.float64)
         twoFX = np.zeros((len(self.multis), len(self.detector_names)))
-        for j, (k, x, _) in enumerate(where):
-            twoFX[k, x] = 2.0 * vals[j]
+        for a, b in chunks_by_cells([n + 1 for _, _, n in where], self.map_budget_cells):
+            _, d_maps, offs = _device_maps_run(tmpl[a:b], self.flags, self.device,
+                                               self.tile_config)
+            idx = np.array([offs[j - a] + where[j][2] for j in range(a, b)], dtype=np.int64)
+            vals = d_maps[torch.from_numpy(idx).to(d_maps.device)].cpu().numpy()
+            for j in range(a, b):
+                k, x, _ = where[j]
+                twoFX[k, x] = 2.0 * float(vals[j - a])
         return twoFX
 
 

@@ -83,3 +83,14 @@ def test_grid_batch_window_none_is_the_full_data_cell():
         assert out["maxTwoF"][k] == out["twoF"][k]
         assert (out["t0_ML"][k], out["tau_ML"][k]) == (m.t0_ML, m.tau_ML)
         assert out["lnBtSG"][k] == pytest.approx(m.lnBtSG, rel=2e-6)
+
+
+def test_grid_batch_in_memory_chunks_equals_one_launch():
+    pts = points(n=6)
+    wr = window(2)
+    one = search.TransientGridBatch(pts, wr, BtSG=True, BSGL=True).run()
+    # a budget of ~2 points' maps forces several launches
+    small = search.TransientGridBatch(pts, window(2), BtSG=True, BSGL=True,
+                                      map_budget_bytes=2 * 4 * 101 * 31).run()
+    for key in one.dtype.names:
+        np.testing.assert_allclose(small[key], one[key], rtol=2e-6, err_msg=key)

@@ -59,3 +59,14 @@ def test_grid_of_window_type_none_is_one_cell_over_all_data():
     assert w == 2 and t0s.size == 11 and taus.size == 8 and taus[-1] == 1800 * 8
     with pytest.raises(ValueError):
         search._grid_for(transientWindowRange_t(type=3), 1800, 0, 10)
+
+
+def test_chunks_by_cells_covers_in_order_within_budget():
+    cells = [5, 3, 9, 1, 1, 12, 4]
+    ch = search.chunks_by_cells(cells, 10)
+    assert ch[0][0] == 0 and ch[-1][1] == len(cells)
+    assert all(b0 == a1 for (_, b0), (a1, _) in zip(ch[:-1], ch[1:]))
+    for a, b in ch:
+        assert b > a and (sum(cells[a:b]) <= 10 or b - a == 1)
+    assert search.chunks_by_cells(cells, float("inf")) == [(0, len(cells))]
+    assert search.chunks_by_cells([], 10) == []
