@@ -66,6 +66,11 @@ struct tcw_plan {
   float *d_atoms_in = nullptr;
   tcw_result *d_res_out = nullptr;
   float *d_maps_out = nullptr;  // maps of tcw_plan_run_maps_host (n_cells floats)
+  // posterior plans: column chunks and the row / column sums
+  uint2 *d_post_chunks = nullptr;
+  uint32_t n_post_chunks = 0;
+  float *d_rowpart = nullptr;
+  double *d_colsum = nullptr;
 };
 
 namespace {
@@ -667,6 +672,8 @@ int tcw_plan_create(tcw_handle *h, const tcw_template_desc *desc, uint32_t n_tem
   p->flags = flags;
   p->n_templates = n_templates;
   p->cfg = cfg;
+  std::vector<uint2> post_chunks;
+  uint64_t post_rows = 0, post_cols = 0;
   std::vector<TemplateDev> T(n_templates);
   std::vector<WorkItem> items;
   std::vector<double> cost;
@@ -699,6 +706,12 @@ int tcw_plan_create(tcw_handle *h, const tcw_template_desc *desc, uint32_t n_tem
       t.t0_off = d.t0_offset;
       t.tau_off = d.tau_offset;
       t.map_off = cells;  // maps of tcw_plan_run_maps: templates in descriptor order
+      t.row_off = post_rows;  // row partials: N_t0 per column chunk
+      t.col_off = post_cols;
+      post_rows += (uint64_t)d.N_t0 * ((d.N_tau + kPostCols - 1u) / kPostCols);
+      post_cols += d.N_tau;
+      if (flags & TCW_FLAG_POSTERIORS)
+        for (uint32_t n0 = 0; n0 < d.N_tau; n0 += kPostCols) post_chunks.push_back(make_uint2(k, n0));
       if (d.window == TCW_WINDOW_RECT) {
         t.p_off = p_rows;
         p_rows += (uint64_t)d.numAtoms + 1u;
@@ -772,6 +785,10 @@ int tcw_plan_create(tcw_handle *h, const tcw_template_desc *desc, uint32_t n_tem
   const size_t o_P = L.add(sizeof(float) * kPrefixStride * std::max<uint64_t>(1, p_rows));
   const size_t o_A8 = L.add(sizeof(float) * 8u * std::max<uint64_t>(1, a8_rows));
   const size_t o_cnt = L.add(2 * sizeof(uint32_t));
+  const bool post = (flags & TCW_FLAG_POSTERIORS) != 0;
+  const size_t o_chunks = post ? L.add(sizeof(uint2) * std::max<size_t>(1, post_chunks.size())) : 0;
+  const size_t o_rowsum = post ? L.add(sizeof(float) * std::max<uint64_t>(1, post_rows)) : 0;
+  const size_t o_colsum = post ? L.add(sizeof(double) * std::max<uint64_t>(1, post_cols)) : 0;
   void *buf = nullptr;
   rc = ws_alloc(h, &buf, L.total);
   if (rc) {
@@ -789,6 +806,12 @@ int tcw_plan_create(tcw_handle *h, const tcw_template_desc *desc, uint32_t n_tem
   p->d_parts = reinterpret_cast<Partial *>(p->d_buf + o_parts);
   p->d_P = reinterpret_cast<float *>(p->d_buf + o_P);
   p->d_counter = reinterpret_cast<uint32_t *>(p->d_buf + o_cnt);
+  if (post) {
+    p->d_post_chunks = reinterpret_cast<uint2 *>(p->d_buf + o_chunks);
+    p->n_post_chunks = (uint32_t)post_chunks.size();
+    p->d_rowpart = reinterpret_cast<float *>(p->d_buf + o_rowsum);
+    p->d_colsum = reinterpret_cast<double *>(p->d_buf + o_colsum);
+  }
   // control data: a synchronous copy (plans are built once)
   std::vector<char> host(ctl_end, 0);
   memcpy(host.data() + o_T, T.data(), sizeof(TemplateDev) * n_templates);
@@ -800,6 +823,9 @@ int tcw_plan_create(tcw_handle *h, const tcw_template_desc *desc, uint32_t n_tem
   memcpy(host.data() + o_t0, t0s, sizeof(uint32_t) * n_t0s);
   memcpy(host.data() + o_tau, taus, sizeof(uint32_t) * n_taus);
   cudaError_t e = cudaMemcpy(p->d_buf, host.data(), ctl_end, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && post && !post_chunks.empty())
+    e = cudaMemcpy(p->d_post_chunks, post_chunks.data(), sizeof(uint2) * post_chunks.size(),
+                   cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     cudaFree(p->d_buf);
     delete p;
@@ -878,7 +904,8 @@ static int plan_enqueue(tcw_handle *h, tcw_plan *p, const float *d_atoms, tcw_re
   TCW_CUDA(h, cudaStreamWaitEvent(h->stream, h->join_ev, 0));
   TCW_CUDA(h, launch_finalize(p->d_T, p->n_templates, p->d_parts, d_results, h->stream));
   if (d_maps && (p->flags & TCW_FLAG_POSTERIORS))
-    TCW_CUDA(h, launch_plan_posteriors(p->d_T, p->n_templates, d_maps, d_results, h->stream));
+    TCW_CUDA(h, launch_plan_posteriors(p->d_T, p->n_templates, p->d_post_chunks, p->n_post_chunks,
+                                       d_maps, d_results, p->d_rowpart, p->d_colsum, h->stream));
   return TCW_OK;
 }
 

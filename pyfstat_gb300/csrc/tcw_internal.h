@@ -32,6 +32,7 @@ struct TemplateDev {
   uint32_t N_t0, N_tau;
   uint32_t part_off, n_parts;
   uint32_t pad;
+  uint64_t row_off, col_off;  // posterior row partials / column sums (plans with posteriors)
 };
 
 // A tile of one template: rows [m0, m1) x columns [n0, n1).  For a
@@ -144,9 +145,15 @@ unsigned int dcheck_failures_kernels();
 unsigned int dcheck_failures_diff();
 unsigned int dcheck_failures_f64();
 unsigned int dcheck_failures_noalloc();
-// Posterior indices of every template of a plan from its written maps.
+// Posterior indices of every template of a plan from its written maps:
+// per column chunk (template, first column; kPostCols columns) one block
+// reads its part of the map once and stores its row partials
+// (d_rowpart + row_off + chunk * N_t0), then one warp per template takes
+// the argmaxes.
+constexpr uint32_t kPostCols = 1024;
 cudaError_t launch_plan_posteriors(const TemplateDev *d_T, uint32_t n_templates,
-                                   const float *d_maps, tcw_result *d_results,
+                                   const uint2 *d_chunks, uint32_t n_chunks, const float *d_maps,
+                                   tcw_result *d_results, float *d_rowpart, double *d_colsum,
                                    cudaStream_t stream);
 // Full-FP64 direct-summation map of rows rows[0..n_rows) (all rows when rows
 // is NULL) into F[r * N_tau + n]; cond optional.

@@ -16,7 +16,7 @@
 //   posterior kernels  row / column sums of exp(F - maxF) over a written map and
 //                    their argmax (t0 / tau max-posterior bins): one template
 //                    (plain path) or every template of a plan
-//                    (plan_posteriors_kernel).
+//                    (post_sums_kernel, post_argmax_kernel).
 // No tensor cores: nothing on this path is a dense contraction.
 #include <math.h>
 #include <stdint.h>
@@ -751,62 +751,100 @@ cudaError_t launch_finalize(const TemplateDev *d_T, uint32_t n_templates, const 
   return cudaGetLastError();
 }
 
-// Batched posteriors of a plan whose maps were written: block k reads
-// template k's map (at map_off) and stores the first-occurrence argmax of
-// the row sums and of the column sums of exp(F - maxF) (tcw:219-287).  Sums
-// in FP32 with Kahan compensation per thread, combined in FP64.
-__global__ void __launch_bounds__(256) plan_posteriors_kernel(const TemplateDev *__restrict__ T,
-                                                              const float *__restrict__ maps,
-                                                              tcw_result *__restrict__ results) {
-  __shared__ double sv[8];
-  __shared__ int64_t si[8];
-  const TemplateDev t = T[blockIdx.x];
-  tcw_result *res = results + blockIdx.x;
-  const float maxF = res->maxF;
+// Batched posteriors of a plan whose maps were written (tcw:219-287): the
+// row and column sums of exp(F - maxF) in one read of the maps.  A block
+// owns kPostCols columns of one template: each thread sums its four
+// adjacent columns down the rows (FP32, Kahan); the block's row sums (the
+// thread's four terms, warp shuffles, then shared memory) are stored per
+// column chunk and summed in FP64 by the argmax kernel (no global atomics).
+constexpr uint32_t kPostRowTile = 1024;
+constexpr uint32_t kPostThreads = 256;  // kPostCols / 4: four adjacent columns per thread
+
+__global__ void __launch_bounds__(kPostThreads) post_sums_kernel(
+    const TemplateDev *__restrict__ T, const uint2 *__restrict__ chunks,
+    const float *__restrict__ maps, const tcw_result *__restrict__ results,
+    float *__restrict__ rowpart, double *__restrict__ colsum) {
+  __shared__ float srow[kPostRowTile];
+  const uint2 ch = chunks[blockIdx.x];
+  const TemplateDev t = T[ch.x];
+  const float maxF = results[ch.x].maxF;
   const float *F = maps + t.map_off;
-  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-  int64_t out_idx[2];
+  const uint32_t n0 = ch.y + 4u * threadIdx.x;  // this thread's first column
+  const uint32_t lane = threadIdx.x & 31u;
+  float *rp = rowpart + t.row_off + (size_t)(ch.y / kPostCols) * t.N_t0;  // this chunk's rows
+  float cs[4] = {0, 0, 0, 0}, cc[4] = {0, 0, 0, 0};
+  for (uint32_t m0 = 0; m0 < t.N_t0; m0 += kPostRowTile) {
+    const uint32_t m1 = min(t.N_t0, m0 + kPostRowTile);
+    for (uint32_t k = threadIdx.x; k < kPostRowTile; k += kPostThreads) srow[k] = 0.0f;
+    __syncthreads();
+    // four rows per step: independent loads and shuffle chains
+    for (uint32_t m = m0; m < m1; m += 4u) {
+      float w[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const uint32_t mq = m + q;
+        const float *row = F + (size_t)mq * t.N_tau;
+        float e[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+          e[j] = (mq < m1 && n0 + j < t.N_tau) ? ex2_approx((row[n0 + j] - maxF) * kLog2e) : 0.0f;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const float y = fsub(e[j], cc[j]);
+          const float u = fadd(cs[j], y);
+          cc[j] = fsub(fsub(u, cs[j]), y);
+          cs[j] = u;
+        }
+        w[q] = fadd(fadd(e[0], e[1]), fadd(e[2], e[3]));
+      }
+#pragma unroll
+      for (int d = 16; d > 0; d >>= 1) {
+#pragma unroll
+        for (int q = 0; q < 4; q++) w[q] += __shfl_xor_sync(0xffffffffu, w[q], d);
+      }
+      if (lane == 0) {
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+          if (m + q < m1 && w[q] != 0.0f) atomicAdd(&srow[m + q - m0], w[q]);
+      }
+    }
+    __syncthreads();
+    for (uint32_t k = threadIdx.x; k < m1 - m0; k += kPostThreads) rp[m0 + k] = srow[k];
+    __syncthreads();
+  }
+#pragma unroll
+  for (int j = 0; j < 4; j++)
+    if (n0 + j < t.N_tau) colsum[t.col_off + n0 + j] = (double)cs[j] - (double)cc[j];
+}
+
+// One warp per template: first-occurrence argmax of its row sums (the
+// column chunks' partials summed in FP64) and of its column sums.
+__global__ void __launch_bounds__(128) post_argmax_kernel(const TemplateDev *__restrict__ T,
+                                                          uint32_t n_templates,
+                                                          const float *__restrict__ rowpart,
+                                                          const double *__restrict__ colsum,
+                                                          tcw_result *__restrict__ results) {
+  const uint32_t tmpl = blockIdx.x * 4u + (threadIdx.x >> 5);
+  const uint32_t lane = threadIdx.x & 31u;
+  if (tmpl >= n_templates) return;
+  const TemplateDev t = T[tmpl];
+  int64_t out[2];
   for (int pass = 0; pass < 2; pass++) {
+    const uint32_t N = pass == 0 ? t.N_t0 : t.N_tau;
+    const uint32_t n_chunks = (t.N_tau + kPostCols - 1u) / kPostCols;
     double best = -1.0;
     int64_t bidx = INT64_MAX;
-    if (pass == 0) {
-      // rows: one warp per row, lanes over columns
-      for (uint32_t m = warp; m < t.N_t0; m += 8u) {
-        const float *row = F + (size_t)m * t.N_tau;
-        float s = 0.0f, c = 0.0f;
-        for (uint32_t n = lane; n < t.N_tau; n += 32u) {
-          const float y = fsub(exp2f((row[n] - maxF) * kLog2e), c);
-          const float u = fadd(s, y);
-          c = fsub(fsub(u, s), y);
-          s = u;
-        }
-        double v = (double)s - (double)c;
-#pragma unroll
-        for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
-        if (v > best) {  // m increases within a warp: keeps the first
-          best = v;
-          bidx = m;
-        }
+    for (uint32_t k = lane; k < N; k += 32u) {
+      double x;
+      if (pass == 0) {
+        x = 0.0;
+        for (uint32_t c = 0; c < n_chunks; c++) x += (double)rowpart[t.row_off + (size_t)c * N + k];
+      } else {
+        x = colsum[t.col_off + k];
       }
-      if (lane != 0) {
-        best = -1.0;
-        bidx = INT64_MAX;
-      }
-    } else {
-      // columns: one thread per column, down all rows
-      for (uint32_t n = threadIdx.x; n < t.N_tau; n += 256u) {
-        float s = 0.0f, c = 0.0f;
-        for (uint32_t m = 0; m < t.N_t0; m++) {
-          const float y = fsub(exp2f((F[(size_t)m * t.N_tau + n] - maxF) * kLog2e), c);
-          const float u = fadd(s, y);
-          c = fsub(fsub(u, s), y);
-          s = u;
-        }
-        const double v = (double)s - (double)c;
-        if (v > best) {
-          best = v;
-          bidx = n;
-        }
+      if (x > best) {  // k increases within a lane: keeps the first
+        best = x;
+        bidx = k;
       }
     }
 #pragma unroll
@@ -818,31 +856,26 @@ __global__ void __launch_bounds__(256) plan_posteriors_kernel(const TemplateDev 
         bidx = oi;
       }
     }
-    if (lane == 0) {
-      sv[warp] = best;
-      si[warp] = bidx;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      for (int w = 1; w < 8; w++)
-        if (sv[w] > best || (sv[w] == best && si[w] < bidx)) {
-          best = sv[w];
-          bidx = si[w];
-        }
-      out_idx[pass] = bidx == INT64_MAX ? -1 : bidx;
-    }
-    __syncthreads();
+    out[pass] = bidx == INT64_MAX ? -1 : bidx;
   }
-  if (threadIdx.x == 0) {
-    res->t0_mp_idx = out_idx[0];
-    res->tau_mp_idx = out_idx[1];
+  if (lane == 0) {
+    results[tmpl].t0_mp_idx = out[0];
+    results[tmpl].tau_mp_idx = out[1];
   }
 }
 
 cudaError_t launch_plan_posteriors(const TemplateDev *d_T, uint32_t n_templates,
-                                   const float *d_maps, tcw_result *d_results,
+                                   const uint2 *d_chunks, uint32_t n_chunks, const float *d_maps,
+                                   tcw_result *d_results, float *d_rowpart, double *d_colsum,
                                    cudaStream_t stream) {
-  plan_posteriors_kernel<<<n_templates, 256, 0, stream>>>(d_T, d_maps, d_results);
+  if (n_chunks) {
+    post_sums_kernel<<<n_chunks, kPostThreads, 0, stream>>>(d_T, d_chunks, d_maps, d_results,
+                                                            d_rowpart, d_colsum);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  post_argmax_kernel<<<(n_templates + 3u) / 4u, 128, 0, stream>>>(d_T, n_templates, d_rowpart,
+                                                                  d_colsum, d_results);
   return cudaGetLastError();
 }
 
