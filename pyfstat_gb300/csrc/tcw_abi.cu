@@ -226,7 +226,8 @@ void tile_template(uint32_t tmpl, const TemplateDev &t, const tcw_tile_config &c
   } else {
     const uint32_t tn = cfg.exp_tn, lanes = kBlock / tn;
     uint32_t rows = cfg.exp_rows ? cfg.exp_rows : N_t0;
-    rows = std::min(rows, N_t0);
+    // a lane's row chunk is a 16-bit count: longer columns become several tiles
+    rows = std::min(std::min(rows, N_t0), 65535u);
     const uint32_t span = rows * lanes;  // rows per block
     for (uint32_t n0 = 0; n0 < N_tau; n0 += tn)
       for (uint32_t m0 = 0; m0 < N_t0; m0 += span) {
@@ -237,7 +238,7 @@ void tile_template(uint32_t tmpl, const TemplateDev &t, const tcw_tile_config &c
         w.n0 = n0;
         w.n1 = std::min(N_tau, n0 + tn);
         w.tn = (uint16_t)tn;
-        w.rows_per_lane = (uint16_t)std::min<uint32_t>(rows, 65535u);
+        w.rows_per_lane = (uint16_t)rows;
         items.push_back(w);
         if (cost) {
           // recurrence steps: window warm-up plus the rows' atom span, per column

@@ -230,3 +230,28 @@ def test_golden_cases_in_one_persistent_launch(oracle, golden):
             assert index_ok(res["t0_mp_idx"][k], e.sum(axis=1)), c["name"]
             assert index_ok(res["tau_mp_idx"][k], e.sum(axis=0)), c["name"]
     batch.close()
+
+
+def test_exp_template_with_more_than_65535_rows(oracle):
+    """Row chunks of exponential tiles are 16-bit counts: a column of 70,000
+    t0 rows must be split, not truncated (plain and batched paths)."""
+    from pyfstat_gb300 import _lib
+
+    t0_data, A = synth.merged_atoms(77, 120, 2, gap_frac=0.05)
+    t0s = (t0_data + 3 * np.arange(70000)).astype(np.uint32)  # 3 s steps over ~58 h
+    taus = np.array([1800, 9000, 36000, 90000], dtype=np.uint32)
+    F64, cond = oracle.map_f64(A, 1800, t0_data, 2, t0s, taus, with_cond=True)
+    band = np.abs(cond / 1e4 - 1) < 1e-5
+    h = _lib.Handle(0)
+    try:
+        F, res = h.map_plain_host(A, 1800, t0_data, 2, t0s, taus, want_map=True)
+        rel = np.where(band, 0, np.abs(F - F64) / np.abs(F64))
+        assert rel.max() < REL_TOL
+        tmpl = dict(atoms=A, TAtom=1800, t0_data=t0_data, window=2, t0s=t0s, taus=taus)
+        b = TransientMapBatch([tmpl], handle=h)
+        r = b.run()[0]
+        b.close()
+        assert abs(float(r["maxF"]) - F64.max()) <= REL_TOL * F64.max()
+        assert argmax_ok(r["argmax"], F64)
+    finally:
+        h.close()
