@@ -255,3 +255,28 @@ def test_exp_template_with_more_than_65535_rows(oracle):
         assert argmax_ok(r["argmax"], F64)
     finally:
         h.close()
+
+
+def test_all_gap_templates_give_the_fallback_everywhere(oracle):
+    """Templates whose atoms are all zero (data gaps only): every cell is the
+    F = 2 fallback, maxF = 2 and lnBtSG = ln 70 + 2, on both paths."""
+    from pyfstat_gb300 import _lib
+
+    A = np.zeros((50, 7), np.float32)
+    t0_data = 700000000
+    t0s = (t0_data + 1800 * np.arange(30)).astype(np.uint32)
+    taus = (1800 + 3600 * np.arange(12)).astype(np.uint32)
+    tl = [dict(atoms=A, TAtom=1800, t0_data=t0_data, window=w, t0s=t0s, taus=taus)
+          for w in (1, 2)]
+    b = TransientMapBatch(tl)
+    res = b.run()
+    for k, w in enumerate((1, 2)):
+        F64 = oracle.map_f64(A, 1800, t0_data, w, t0s, taus)
+        assert np.all(F64 == 2.0)
+        F, r = b.handle.map_plain_host(A, 1800, t0_data, w, t0s, taus, want_map=True,
+                                       flags=_lib.TCW_FLAG_LNBTSG)
+        assert np.all(F == 2.0)
+        for rec in (r, res[k]):
+            assert float(rec["maxF"]) == 2.0 and int(rec["argmax"]) == 0
+            assert float(rec["lnBtSG"]) == pytest.approx(np.log(70.0) + 2.0, rel=1e-12)
+    b.close()
