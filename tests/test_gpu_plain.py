@@ -200,3 +200,37 @@ def test_drop_in_dispatcher(oracle):
     finally:
         if ctx:
             ctx.detach()
+
+
+def test_maps_differ_from_the_reference_maps_only_by_its_own_rounding(handle, oracle, golden):
+    """Against the reference's own outputs (its pycuda kernels' FP32 maps in
+    the golden file): every cell of the GPU map lies within the reference's
+    own distance from FP64 plus 1e-5 relative of it -- the two differ only
+    by the reference's FP32 rounding."""
+    names = sorted({k.split("__")[0] for k in golden.files})
+    worst_ref = 0.0
+    for name in names:
+        g = golden[f"{name}__grid"]
+        window, TAtom, t0_data = int(g[0]), int(g[1]), int(g[2])
+        if f"{name}__t0s" in golden.files:
+            t0s, taus = golden[f"{name}__t0s"], golden[f"{name}__taus"]
+        else:
+            c = golden_case(golden, name)
+            t0s, taus = c["t0s"], c["taus"]
+        A = golden[f"{name}__atoms"]
+        F, _ = handle.map_plain_host(A, TAtom, t0_data, window, t0s, taus, want_map=True)
+        F64, cond = oracle.map_f64(A, TAtom, t0_data, window if window else 1,
+                                   t0s if window else np.array([t0_data], np.uint32),
+                                   taus if window else np.array([A.shape[0] * TAtom], np.uint32),
+                                   with_cond=True)
+        if f"{name}__F" in golden.files:
+            Fref, rows = golden[f"{name}__F"], slice(None)
+        else:
+            Fref, rows = golden[f"{name}__F_rows16"], slice(None, None, 16)
+        Fg, F64r, cr = F[rows].astype(np.float64), F64[rows], cond[rows]
+        band = np.abs(cr / 1e4 - 1.0) < 1e-5
+        ref_err = np.abs(Fref.astype(np.float64) - F64r)
+        ok = np.abs(Fg - Fref) <= ref_err + REL_TOL * np.abs(F64r) + 1e-12
+        assert np.all(ok | band), name
+        worst_ref = max(worst_ref, float(np.max(np.where(band, 0, ref_err / np.abs(F64r)))))
+    print(f"\nreference FP32 maps' own max rel err vs FP64 over the golden cases: {worst_ref:.3e}")
