@@ -164,6 +164,15 @@ int tcw_plan_run_maps(tcw_handle *h, tcw_plan *plan, const float *d_atoms, tcw_r
  * maps (tcw:219-287); such a plan only runs through the _maps entry points. */
 int tcw_plan_run_maps_host(tcw_handle *h, tcw_plan *plan, const float *atoms, tcw_result *results,
                            float *maps);
+/* One-shot batched call on host buffers (plan, run, results, release):
+ * per template max2F (2 maxF), the flat argmax and lnBtSG -- the batched
+ * entry a transient grid search calls once instead of one map per Doppler
+ * point (grid_based_searches.py:1186-1189).  Output arrays hold n_templates
+ * values; cfg may be NULL (library tiles). */
+int tcw_map_batched(tcw_handle *h, const tcw_template_desc *desc, uint32_t n_templates,
+                    const uint32_t *t0s, uint64_t n_t0s, const uint32_t *taus, uint64_t n_taus,
+                    const float *atoms_concat, const tcw_tile_config *cfg, float *max2F,
+                    int64_t *argmax, double *lnBtSG);
 /* One run without a graph and with the two map kernels one after the other,
  * CUDA events between the kernels on the handle's stream; synchronises and
  * writes the durations (ms) of the prefix, rectangular-map, exponential-map

@@ -96,6 +96,8 @@ SIGNATURES = {
     "tcw_plan_info": (ctypes.c_int, [_vp, ctypes.POINTER(_c_u64), ctypes.POINTER(_c_u32),
                                      ctypes.POINTER(_c_u64), ctypes.POINTER(TcwTileConfig)]),
     "tcw_plan_run": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int]),
+    "tcw_map_batched": (ctypes.c_int, [_vp, _vp, _c_u32, _vp, _c_u64, _vp, _c_u64, _vp,
+                                       ctypes.POINTER(TcwTileConfig), _vp, _vp, _vp]),
     "tcw_plan_run_maps": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, ctypes.c_int]),
     "tcw_plan_run_maps_host": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp]),
     "tcw_plan_run_host": (ctypes.c_int, [_vp, _vp, _vp, _vp]),

@@ -99,3 +99,22 @@ class TransientMapBatch:
 
     def close(self):
         self.plan.close()
+
+
+def map_batched(templates, handle=None, device=0):
+    """One-shot batched maps through the C ABI's ``tcw_map_batched`` (host
+    buffers; no plan kept): (max2F float32, argmax int64, lnBtSG float64)
+    per template."""
+    import ctypes
+
+    atoms, desc, t0s, taus = pack_templates(templates)
+    h = handle if handle is not None else _lib.Handle(device)
+    n = desc.shape[0]
+    max2F = np.empty(n, dtype=np.float32)
+    argmax = np.empty(n, dtype=np.int64)
+    lnB = np.empty(n, dtype=np.float64)
+    _lib.check(_lib.load().tcw_map_batched(
+        h.ptr, desc.ctypes.data, n, t0s.ctypes.data, t0s.shape[0], taus.ctypes.data,
+        taus.shape[0], atoms.ctypes.data, ctypes.POINTER(_lib.TcwTileConfig)(),
+        max2F.ctypes.data, argmax.ctypes.data, lnB.ctypes.data), h.ptr)
+    return max2F, argmax, lnB

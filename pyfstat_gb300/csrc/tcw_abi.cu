@@ -1246,6 +1246,35 @@ int tcw_plan_run_maps_host(tcw_handle *h, tcw_plan *p, const float *atoms, tcw_r
   return TCW_OK;
 }
 
+int tcw_map_batched(tcw_handle *h, const tcw_template_desc *desc, uint32_t n_templates,
+                    const uint32_t *t0s, uint64_t n_t0s, const uint32_t *taus, uint64_t n_taus,
+                    const float *atoms_concat, const tcw_tile_config *cfg, float *max2F,
+                    int64_t *argmax, double *lnBtSG) {
+  if (!h) return TCW_ERR_INVALID_ARG;
+  if (!atoms_concat || !max2F || !argmax || !lnBtSG)
+    return set_err(h, TCW_ERR_INVALID_ARG, "null host pointer");
+  tcw_plan *p = nullptr;
+  int rc = tcw_plan_create(h, desc, n_templates, t0s, n_t0s, taus, n_taus, cfg, TCW_FLAG_LNBTSG,
+                           &p);
+  if (rc) return rc;
+  std::vector<tcw_result> res;
+  try {
+    res.resize(n_templates);
+  } catch (const std::bad_alloc &) {
+    tcw_plan_destroy(p);
+    return set_err(h, TCW_ERR_ALLOC, "host allocation failed");
+  }
+  rc = tcw_plan_run_host(h, p, atoms_concat, res.data());
+  tcw_plan_destroy(p);
+  if (rc) return rc;
+  for (uint32_t k = 0; k < n_templates; k++) {
+    max2F[k] = 2.0f * res[k].maxF;
+    argmax[k] = res[k].argmax;
+    lnBtSG[k] = res[k].lnBtSG;
+  }
+  return TCW_OK;
+}
+
 int tcw_debug_check_failures(uint32_t *count) {
   if (!count) return TCW_ERR_INVALID_ARG;
   uint64_t n = (uint64_t)dcheck_failures_kernels() + dcheck_failures_diff() +

@@ -280,3 +280,13 @@ def test_all_gap_templates_give_the_fallback_everywhere(oracle):
             assert float(rec["maxF"]) == 2.0 and int(rec["argmax"]) == 0
             assert float(rec["lnBtSG"]) == pytest.approx(np.log(70.0) + 2.0, rel=1e-12)
     b.close()
+
+
+def test_one_shot_map_batched_equals_the_plan(batch):
+    from pyfstat_gb300.batched import map_batched
+
+    res = batch.run()
+    max2F, argmax, lnB = map_batched(small_templates(), handle=batch.handle)
+    assert np.array_equal(max2F, 2.0 * res["maxF"])
+    assert np.array_equal(argmax, res["argmax"])
+    assert np.array_equal(lnB, res["lnBtSG"])
