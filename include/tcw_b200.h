@@ -180,8 +180,8 @@ int tcw_map_batched(tcw_handle *h, const tcw_template_desc *desc, uint32_t n_tem
 int tcw_plan_run_timed(tcw_handle *h, tcw_plan *plan, const float *d_atoms, tcw_result *d_results,
                        float *ms);
 
-/* Differentiable maps, exponential or rectangular windows (desc.window; the
- * "expdiff" names are historical) -- no counterpart in the reference: an
+/* Differentiable maps, exponential or rectangular windows (desc.window) --
+ * no counterpart in the reference: an
  * addition for gradient-based searches.  Per template the tau grid is
  * continuous, tau_n = tau_min + n (tau_max - tau_min) / (N_tau - 1); the
  * t0 grid (host array, seconds) must be non-decreasing and start no earlier
@@ -201,18 +201,18 @@ typedef struct {
   double tau_max;
 } tcw_diff_desc;
 
-int tcw_expdiff_forward(tcw_handle *h, const tcw_diff_desc *desc, uint32_t n_templates,
-                        const float *d_atoms, const uint32_t *t0s, uint64_t n_t0s,
-                        double temperature, double *d_lnBtSG, double *d_softmax2F);
+int tcw_map_forward(tcw_handle *h, const tcw_diff_desc *desc, uint32_t n_templates,
+                    const float *d_atoms, const uint32_t *t0s, uint64_t n_t0s,
+                    double temperature, double *d_lnBtSG, double *d_softmax2F);
 /* Gradients of L(lnBtSG, softmax2F) given dL/dlnBtSG and dL/dsoftmax2F per
  * template (device arrays) and the forward's outputs: d_grad_atoms
  * (n_atom_rows x 7, FP64, overwritten) and d_grad_tau (n_templates x 2:
  * dL/dtau_min, dL/dtau_max, overwritten).  Recomputes the window sums. */
-int tcw_expdiff_backward(tcw_handle *h, const tcw_diff_desc *desc, uint32_t n_templates,
-                         const float *d_atoms, const uint32_t *t0s, uint64_t n_t0s,
-                         double temperature, const double *d_lnBtSG, const double *d_softmax2F,
-                         const double *d_grad_lnBtSG, const double *d_grad_softmax2F,
-                         double *d_grad_atoms, uint64_t n_atom_rows, double *d_grad_tau);
+int tcw_map_backward(tcw_handle *h, const tcw_diff_desc *desc, uint32_t n_templates,
+                     const float *d_atoms, const uint32_t *t0s, uint64_t n_t0s,
+                     double temperature, const double *d_lnBtSG, const double *d_softmax2F,
+                     const double *d_grad_lnBtSG, const double *d_grad_softmax2F,
+                     double *d_grad_atoms, uint64_t n_atom_rows, double *d_grad_tau);
 
 /* Device-side index checks of a debug build (compiled with -DTCW_DEBUG_CHECKS:
  * every index of a map / adjoint / reference kernel load or store is checked

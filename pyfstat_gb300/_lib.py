@@ -108,9 +108,9 @@ SIGNATURES = {
     "tcw_debug_check_failures": (ctypes.c_int, [ctypes.POINTER(_c_u32)]),
     "tcw_map_f64": (ctypes.c_int, [_vp, _vp, _c_u32, _c_u32, _c_u32, ctypes.c_int, _vp, _c_u32,
                                    _vp, _c_u32, _vp, _c_u32, _vp, _vp]),
-    "tcw_expdiff_forward": (ctypes.c_int, [_vp, _vp, _c_u32, _vp, _vp, _c_u64, ctypes.c_double,
+    "tcw_map_forward": (ctypes.c_int, [_vp, _vp, _c_u32, _vp, _vp, _c_u64, ctypes.c_double,
                                            _vp, _vp]),
-    "tcw_expdiff_backward": (ctypes.c_int, [_vp, _vp, _c_u32, _vp, _vp, _c_u64, ctypes.c_double,
+    "tcw_map_backward": (ctypes.c_int, [_vp, _vp, _c_u32, _vp, _vp, _c_u64, ctypes.c_double,
                                             _vp, _vp, _vp, _vp, _vp, _c_u64, _vp]),
     "tcw_write_map_text": (ctypes.c_int, [ctypes.c_char_p, _vp, _c_u32, _c_u32, _vp, _vp,
                                           ctypes.c_int]),

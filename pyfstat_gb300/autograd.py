@@ -77,7 +77,7 @@ class DiffBatch:
         lnB = torch.empty(self.n_templates, dtype=torch.float64, device=dev)
         soft = torch.empty(self.n_templates, dtype=torch.float64, device=dev)
         self._stream()
-        _lib.check(_lib.load().tcw_expdiff_forward(
+        _lib.check(_lib.load().tcw_map_forward(
             self.handle.ptr, d.ctypes.data, self.n_templates, d_atoms.data_ptr(),
             self.t0s.ctypes.data, self.t0s.shape[0], self.temperature, lnB.data_ptr(),
             soft.data_ptr()), self.handle.ptr)
@@ -92,7 +92,7 @@ class DiffBatch:
         g_lnB = g_lnB.to(torch.float64).contiguous()
         g_soft = g_soft.to(torch.float64).contiguous()
         self._stream()
-        _lib.check(_lib.load().tcw_expdiff_backward(
+        _lib.check(_lib.load().tcw_map_backward(
             self.handle.ptr, d.ctypes.data, self.n_templates, d_atoms.data_ptr(),
             self.t0s.ctypes.data, self.t0s.shape[0], self.temperature, lnB.data_ptr(),
             soft.data_ptr(), g_lnB.data_ptr(), g_soft.data_ptr(), ga.data_ptr(), self.n_rows,

@@ -1129,9 +1129,9 @@ static DiffLaunch diff_launch(tcw_handle *h, const DiffSetup &S, const float *d_
   return L;
 }
 
-int tcw_expdiff_forward(tcw_handle *h, const tcw_diff_desc *desc, uint32_t n_templates,
-                        const float *d_atoms, const uint32_t *t0s, uint64_t n_t0s,
-                        double temperature, double *d_lnBtSG, double *d_softmax2F) {
+int tcw_map_forward(tcw_handle *h, const tcw_diff_desc *desc, uint32_t n_templates,
+                    const float *d_atoms, const uint32_t *t0s, uint64_t n_t0s,
+                    double temperature, double *d_lnBtSG, double *d_softmax2F) {
   if (!h) return TCW_ERR_INVALID_ARG;
   if (!d_atoms || !d_lnBtSG || !d_softmax2F)
     return set_err(h, TCW_ERR_INVALID_ARG, "null device pointer");
@@ -1148,11 +1148,11 @@ int tcw_expdiff_forward(tcw_handle *h, const tcw_diff_desc *desc, uint32_t n_tem
   return TCW_OK;
 }
 
-int tcw_expdiff_backward(tcw_handle *h, const tcw_diff_desc *desc, uint32_t n_templates,
-                         const float *d_atoms, const uint32_t *t0s, uint64_t n_t0s,
-                         double temperature, const double *d_lnBtSG, const double *d_softmax2F,
-                         const double *d_grad_lnBtSG, const double *d_grad_softmax2F,
-                         double *d_grad_atoms, uint64_t n_atom_rows, double *d_grad_tau) {
+int tcw_map_backward(tcw_handle *h, const tcw_diff_desc *desc, uint32_t n_templates,
+                     const float *d_atoms, const uint32_t *t0s, uint64_t n_t0s,
+                     double temperature, const double *d_lnBtSG, const double *d_softmax2F,
+                     const double *d_grad_lnBtSG, const double *d_grad_softmax2F,
+                     double *d_grad_atoms, uint64_t n_atom_rows, double *d_grad_tau) {
   if (!h) return TCW_ERR_INVALID_ARG;
   if (!d_atoms || !d_lnBtSG || !d_softmax2F || !d_grad_lnBtSG || !d_grad_softmax2F ||
       !d_grad_atoms || !d_grad_tau)
