@@ -477,7 +477,7 @@ TCW_HD bool fstat_fast(const FF W[7], float &F) {
                          fadd(W[6].h, W[6].l), F);
 }
 
-// Window sums held as four channel pairs (A,B) (C,Fa_re) (Fa_im,Fb_re)
+// Rectangular window sums held as four channel pairs (A,B) (C,Fa_re) (Fa_im,Fb_re)
 // (Fb_im,-): unpack to seven double-words.
 TCW_HD void ff2_unpack(const FF2 P[4], FF W[7]) {
   W[0] = FF{P[0].h.x, P[0].l.x};
@@ -501,6 +501,37 @@ TCW_HD float fstat_tiered2(const FF2 P[4], bool &ok) {
   }
   FF W[7];
   ff2_unpack(P, W);
+  return fstat_ff<kFp64Det>(W[0], W[1], W[2], W[3], W[4], W[5], W[6], ok);
+}
+
+// Exponential columns pair the channels by decay ratio instead: (A,B) and
+// (C,-) decay with r^2, (Fa_re,Fa_im) and (Fb_re,Fb_im) with r, so each
+// packed pair has one ratio in both lanes.  Atom rows of 8 floats hold the
+// channels in that order: [a2 b2 ab 0 Fa_re Fa_im Fb_re Fb_im]; kRow8Slot[c]
+// is the slot of channel c (a2 b2 ab Fa_re Fa_im Fb_re Fb_im).
+constexpr int kRow8Slot[7] = {0, 1, 2, 4, 5, 6, 7};
+
+TCW_HD void ff2_unpack_row8(const FF2 P[4], FF W[7]) {
+  W[0] = FF{P[0].h.x, P[0].l.x};
+  W[1] = FF{P[0].h.y, P[0].l.y};
+  W[2] = FF{P[1].h.x, P[1].l.x};
+  W[3] = FF{P[2].h.x, P[2].l.x};
+  W[4] = FF{P[2].h.y, P[2].l.y};
+  W[5] = FF{P[3].h.x, P[3].l.x};
+  W[6] = FF{P[3].h.y, P[3].l.y};
+}
+
+template <bool kFp64Det>
+TCW_HD float fstat_tiered_row8(const FF2 P[4], bool &ok) {
+  const F2 s0 = add2(P[0].h, P[0].l), s1 = add2(P[1].h, P[1].l);
+  const F2 s2 = add2(P[2].h, P[2].l), s3 = add2(P[3].h, P[3].l);
+  float F;
+  if (fstat_fast_sums(s0.x, s0.y, s1.x, s2.x, s2.y, s3.x, s3.y, F)) {
+    ok = true;
+    return F;
+  }
+  FF W[7];
+  ff2_unpack_row8(P, W);
   return fstat_ff<kFp64Det>(W[0], W[1], W[2], W[3], W[4], W[5], W[6], ok);
 }
 
@@ -829,9 +860,11 @@ TCW_HD void exp_column(const float *__restrict__ atoms, const Geom &g,
 
 // ------------------------------------------------------------ packed exponential column
 // The same column walk as exp_column with the seven channels in four packed
-// pairs and the atoms in 32-byte rows [a2 b2 ab Fa_re Fa_im Fb_re Fb_im 0]
-// (one 256-bit load per recurrence step on the device).  Pair k of the
-// state runs with the pair of ratios (r2 r2) (r2 r1) (r1 r1) (r1 0).
+// pairs and the atoms in 32-byte rows [a2 b2 ab 0 Fa_re Fa_im Fb_re Fb_im]
+// (one 256-bit load per recurrence step on the device).  Pairs 0 and 1 of
+// the state run with the ratio r^2 in both lanes, pairs 2 and 3 with r, so
+// the per-column constants are two packed ratios (and two packed tail
+// factors) rather than four.
 TCW_HD void load_row8(const float *__restrict__ p, F2 x[4]) {
 #if defined(__CUDA_ARCH__)
   asm volatile("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
@@ -843,17 +876,18 @@ TCW_HD void load_row8(const float *__restrict__ p, F2 x[4]) {
 #endif
 }
 
+// Index 0: r^2 (pairs 0, 1); index 1: r (pairs 2, 3).
 struct ExpConsts2 {
-  F2 rh[4], nrh[4], rl[4];
+  F2 rh[2], nrh[2], rl[2];
 };
 
 TCW_HD ExpConsts2 exp_consts2(const ExpConsts &k) {
   ExpConsts2 c;
-  const FF r[4][2] = {{k.r2, k.r2}, {k.r2, k.r1}, {k.r1, k.r1}, {k.r1, FF{0.0f, 0.0f}}};
-  for (int i = 0; i < 4; i++) {
-    c.rh[i] = F2{r[i][0].h, r[i][1].h};
-    c.nrh[i] = F2{-r[i][0].h, -r[i][1].h};
-    c.rl[i] = F2{r[i][0].l, r[i][1].l};
+  const FF r[2] = {k.r2, k.r1};
+  for (int i = 0; i < 2; i++) {
+    c.rh[i] = F2{r[i].h, r[i].h};
+    c.nrh[i] = F2{-r[i].h, -r[i].h};
+    c.rl[i] = F2{r[i].l, r[i].l};
   }
   return c;
 }
@@ -894,7 +928,7 @@ TCW_HD void exp_column2(const float *__restrict__ atoms8, const Geom &g,
   uint32_t nz = 0xFFFFFFFFu;  // first atom >= jL with a2 or b2 non-zero
   uint32_t Lp = 0;            // exponent of the cached power pw = r1^Lp
   FF pw{1.0f, 0.0f};
-  F2 ph[4], nph[4], pl[4];     // per-pair tail factors for the current Lp
+  F2 ph[2], nph[2], pl[2];     // tail factors r^(2 Lp), r^Lp (packed) for the current Lp
   bool pinit = false;
   bool init = false;
   for (uint32_t mm = m_end; mm > m_begin; mm--) {
@@ -920,7 +954,8 @@ TCW_HD void exp_column2(const float *__restrict__ atoms8, const Geom &g,
       TCW_DCHECK(jH < g.numAtoms);
       load_row8(atoms8 + (size_t)jH * 8u, x);
 #pragma unroll
-      for (int c = 0; c < 4; c++) Ehi[c] = ff2_axpy(x[c], k2.rh[c], k2.nrh[c], k2.rl[c], Ehi[c]);
+      for (int c = 0; c < 4; c++)
+        Ehi[c] = ff2_axpy(x[c], k2.rh[c >> 1], k2.nrh[c >> 1], k2.rl[c >> 1], Ehi[c]);
     }
     while (jL > lo) {
       jL--;
@@ -928,7 +963,8 @@ TCW_HD void exp_column2(const float *__restrict__ atoms8, const Geom &g,
       TCW_DCHECK(jL < g.numAtoms);
       load_row8(atoms8 + (size_t)jL * 8u, x);
 #pragma unroll
-      for (int c = 0; c < 4; c++) Elo[c] = ff2_axpy(x[c], k2.rh[c], k2.nrh[c], k2.rl[c], Elo[c]);
+      for (int c = 0; c < 4; c++)
+        Elo[c] = ff2_axpy(x[c], k2.rh[c >> 1], k2.nrh[c >> 1], k2.rl[c >> 1], Elo[c]);
       if (x[0].x != 0.0f || x[0].y != 0.0f) nz = jL;
     }
     if (nz > hi) {  // no data in the window: zero sums, cond = inf
@@ -938,7 +974,7 @@ TCW_HD void exp_column2(const float *__restrict__ atoms8, const Geom &g,
     bool ok;
     float F;
     if (top == J) {
-      F = fstat_tiered2<kFp64Det>(Elo, ok);
+      F = fstat_tiered_row8<kFp64Det>(Elo, ok);
     } else {
       const uint32_t L = top - lo;
       if (L != Lp || !pinit) {
@@ -953,28 +989,25 @@ TCW_HD void exp_column2(const float *__restrict__ atoms8, const Geom &g,
         const FF p2 = ff_mul(pw, pw);
         ph[0] = F2{p2.h, p2.h};
         pl[0] = F2{p2.l, p2.l};
-        ph[1] = F2{p2.h, pw.h};
-        pl[1] = F2{p2.l, pw.l};
-        ph[2] = F2{pw.h, pw.h};
-        pl[2] = F2{pw.l, pw.l};
-        ph[3] = F2{pw.h, pw.h};
-        pl[3] = F2{pw.l, pw.l};
+        ph[1] = F2{pw.h, pw.h};
+        pl[1] = F2{pw.l, pw.l};
 #pragma unroll
-        for (int c = 0; c < 4; c++) nph[c] = F2{-ph[c].x, -ph[c].y};
+        for (int c = 0; c < 2; c++) nph[c] = F2{-ph[c].x, -ph[c].y};
       }
       FF2 W[4];
 #pragma unroll
-      for (int c = 0; c < 4; c++) W[c] = ff2_sub_scaled_fast(Elo[c], ph[c], nph[c], pl[c], Ehi[c]);
+      for (int c = 0; c < 4; c++)
+        W[c] = ff2_sub_scaled_fast(Elo[c], ph[c >> 1], nph[c >> 1], pl[c >> 1], Ehi[c]);
       const F2 s0 = add2(W[0].h, W[0].l), s1 = add2(W[1].h, W[1].l);
       const F2 s2 = add2(W[2].h, W[2].l), s3 = add2(W[3].h, W[3].l);
-      if (fstat_fast_sums(s0.x, s0.y, s1.x, s1.y, s2.x, s2.y, s3.x, F)) {
+      if (fstat_fast_sums(s0.x, s0.y, s1.x, s2.x, s2.y, s3.x, s3.y, F)) {
         ok = true;
       } else {
 #pragma unroll
         for (int c = 0; c < 4; c++)
-          W[c] = ff2_sub_scaled_exact(Elo[c], ph[c], nph[c], pl[c], Ehi[c]);
+          W[c] = ff2_sub_scaled_exact(Elo[c], ph[c >> 1], nph[c >> 1], pl[c >> 1], Ehi[c]);
         FF Ws[7];
-        ff2_unpack(W, Ws);
+        ff2_unpack_row8(W, Ws);
         F = fstat_ff<kFp64Det>(Ws[0], Ws[1], Ws[2], Ws[3], Ws[4], Ws[5], Ws[6], ok);
       }
     }

@@ -65,8 +65,9 @@ __global__ void __launch_bounds__(256) repack_kernel(const TemplateDev *__restri
   float4 *o = reinterpret_cast<float4 *>(A8 + t.a8_off * 8u);
   for (uint32_t i = threadIdx.x; i < t.g.numAtoms; i += blockDim.x) {
     const float *r = x + (size_t)i * 7u;
-    o[2u * i] = make_float4(__ldg(r), __ldg(r + 1), __ldg(r + 2), __ldg(r + 3));
-    o[2u * i + 1u] = make_float4(__ldg(r + 4), __ldg(r + 5), __ldg(r + 6), 0.0f);
+    // row layout kRow8Slot: [a2 b2 ab 0 Fa_re Fa_im Fb_re Fb_im]
+    o[2u * i] = make_float4(__ldg(r), __ldg(r + 1), __ldg(r + 2), 0.0f);
+    o[2u * i + 1u] = make_float4(__ldg(r + 3), __ldg(r + 4), __ldg(r + 5), __ldg(r + 6));
   }
 }
 

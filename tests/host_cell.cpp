@@ -93,7 +93,7 @@ int hc_exp_map(const float *atoms, uint32_t n, uint32_t TAtom, uint32_t t0_data,
   float *a8 = (float *)calloc((size_t)n * 8u, sizeof(float));
   if (!a8) return -1;
   for (uint32_t i = 0; i < n; i++)
-    for (int c = 0; c < 7; c++) a8[(size_t)i * 8u + c] = atoms[(size_t)i * 7u + c];
+    for (int c = 0; c < 7; c++) a8[(size_t)i * 8u + kRow8Slot[c]] = atoms[(size_t)i * 7u + c];
   for (uint32_t k = 0; k < N_tau; k++) {
     for (uint32_t mb = 0; mb < N_t0; mb += row_chunk) {
       uint32_t me = mb + row_chunk < N_t0 ? mb + row_chunk : N_t0;
