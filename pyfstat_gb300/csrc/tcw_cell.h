@@ -892,43 +892,48 @@ TCW_HD ExpConsts2 exp_consts2(const ExpConsts &k) {
   return c;
 }
 
-// E1 - p*E2 per lane with only the high-word subtraction rounding (see
-// ff_sub_scaled_fast); np_h = -p.h.
-TCW_HD FF2 ff2_sub_scaled_fast(FF2 E1, F2 ph, F2 nph, F2 pl, FF2 E2) {
-  const F2 na = mul2(nph, E2.h);
-  F2 ae = fma2(ph, E2.h, na);
-  ae = fma2(ph, E2.l, ae);
-  ae = fma2(pl, E2.h, ae);
-  return FF2{add2(E1.h, na), sub2(E1.l, ae)};
+// W - p*x per lane for a double-word W, a packed double-word factor p
+// (ph + pl, nph = -ph) and single-word x: the product's rounding error is
+// formed exactly (FMA) and the high-word subtraction is a TwoSum, so the
+// result is a double-word as accurate as an ff2_axpy step.
+TCW_HD FF2 ff2_sub_scaled_x(FF2 W, F2 ph, F2 nph, F2 pl, F2 x) {
+  const F2 na = mul2(nph, x);        // -a, a = fl(p.h x)
+  F2 ae = fma2(ph, x, na);           // p.h x - a exactly
+  ae = fma2(pl, x, ae);              // + p.l x
+  const F2 s = add2(W.h, na);        // TwoSum(W.h, -a)
+  const F2 bb = sub2(s, W.h);
+  const F2 e = add2(sub2(W.h, sub2(s, bb)), sub2(na, bb));
+  return FF2{s, sub2(add2(e, W.l), ae)};
 }
 
-// The same with an exact (TwoSum) high-word subtraction (tier 2).
-TCW_HD FF2 ff2_sub_scaled_exact(FF2 E1, F2 ph, F2 nph, F2 pl, FF2 E2) {
-  const F2 na = mul2(nph, E2.h);
-  F2 ae = fma2(ph, E2.h, na);
-  ae = fma2(ph, E2.l, ae);
-  ae = fma2(pl, E2.h, ae);
-  const F2 s = add2(E1.h, na);
-  const F2 bb = sub2(s, E1.h);
-  const F2 e = add2(sub2(E1.h, sub2(s, bb)), sub2(na, bb));
-  return FF2{s, sub2(add2(e, E1.l), ae)};
-}
-
+// One sliding window sum per column.  W holds, for the atom range
+// [wlo, wtop), sum_i x_i r^(i - wlo) (r^2 for A, B, C): the common factor
+// e^(-k (t_wlo - t0)/tau) of the exponential weights is dropped as in
+// exp_column.  Moving to the next (lower) row's window [lo, top):
+//   * an atom i leaving at the top is removed with its current weight
+//     r^(i - wlo) (a cached double-word power, updated by one
+//     multiplication when the exponent moves by one);
+//   * an atom entering at the bottom is added by W = x + r W.
+// Every step is a double-word operation with an exact product error and a
+// TwoSum, so W stays within a few eps^2 of the exact window sum of the
+// recurrence's weights.  If the next window is not reachable that way (it
+// lies above wlo or wtop, only with u32 wrap-around in the grid, or it does
+// not overlap the current one), W restarts empty at the new window's top.
 template <bool kFp64Det, class Sink>
 TCW_HD void exp_column2(const float *__restrict__ atoms8, const Geom &g,
                         const uint32_t *__restrict__ t0s, uint32_t m_begin, uint32_t m_end,
                         uint32_t tau, Sink &sink, const uint32_t *lo_tab = nullptr) {
   const ExpConsts k = exp_consts(g.TAtom, tau);
   const ExpConsts2 k2 = exp_consts2(k);
-  FF2 Elo[4], Ehi[4];
+  FF2 W[4];
   const F2 z{0.0f, 0.0f};
 #pragma unroll
-  for (int c = 0; c < 4; c++) Elo[c] = Ehi[c] = FF2{z, z};
-  uint32_t J = 0, jL = 0, jH = 0;
-  uint32_t nz = 0xFFFFFFFFu;  // first atom >= jL with a2 or b2 non-zero
-  uint32_t Lp = 0;            // exponent of the cached power pw = r1^Lp
+  for (int c = 0; c < 4; c++) W[c] = FF2{z, z};
+  uint32_t wlo = 0, wtop = 0;
+  uint32_t nz = 0xFFFFFFFFu;  // lowest atom >= wlo with a2 or b2 non-zero
+  uint32_t Lp = 0;            // exponent of the cached power pw = r^Lp
   FF pw{1.0f, 0.0f};
-  F2 ph[2], nph[2], pl[2];     // tail factors r^(2 Lp), r^Lp (packed) for the current Lp
+  F2 ph[2], nph[2], pl[2];    // r^(2 Lp) and r^Lp, packed
   bool pinit = false;
   bool init = false;
   for (uint32_t mm = m_end; mm > m_begin; mm--) {
@@ -941,50 +946,24 @@ TCW_HD void exp_column2(const float *__restrict__ atoms8, const Geom &g,
       continue;
     }
     const uint32_t top = hi + 1u;
-    if (!init || top > J || lo > jL || top > jH) {
-      J = jL = jH = top;
+    if (!init || top > wtop || lo > wlo || top <= wlo) {
+      wlo = wtop = top;
       nz = 0xFFFFFFFFu;
 #pragma unroll
-      for (int c = 0; c < 4; c++) Elo[c] = Ehi[c] = FF2{z, z};
+      for (int c = 0; c < 4; c++) W[c] = FF2{z, z};
       init = true;
     }
-    while (jH > top) {
-      jH--;
-      F2 x[4];
-      TCW_DCHECK(jH < g.numAtoms);
-      load_row8(atoms8 + (size_t)jH * 8u, x);
-#pragma unroll
-      for (int c = 0; c < 4; c++)
-        Ehi[c] = ff2_axpy(x[c], k2.rh[c >> 1], k2.nrh[c >> 1], k2.rl[c >> 1], Ehi[c]);
-    }
-    while (jL > lo) {
-      jL--;
-      F2 x[4];
-      TCW_DCHECK(jL < g.numAtoms);
-      load_row8(atoms8 + (size_t)jL * 8u, x);
-#pragma unroll
-      for (int c = 0; c < 4; c++)
-        Elo[c] = ff2_axpy(x[c], k2.rh[c >> 1], k2.nrh[c >> 1], k2.rl[c >> 1], Elo[c]);
-      if (x[0].x != 0.0f || x[0].y != 0.0f) nz = jL;
-    }
-    if (nz > hi) {  // no data in the window: zero sums, cond = inf
-      sink(m, 2.0f, false);
-      continue;
-    }
-    bool ok;
-    float F;
-    if (top == J) {
-      F = fstat_tiered_row8<kFp64Det>(Elo, ok);
-    } else {
-      const uint32_t L = top - lo;
-      if (L != Lp || !pinit) {
-        if (pinit && L == Lp + 1u)
+    while (wtop > top) {
+      wtop--;
+      const uint32_t e = wtop - wlo;  // weight exponent of the leaving atom
+      if (e != Lp || !pinit) {
+        if (pinit && e == Lp + 1u)
           pw = ff_mul(pw, k.r1);
-        else if (pinit && L + 1u == Lp && k.has_inv)
+        else if (pinit && e + 1u == Lp && k.has_inv)
           pw = ff_mul(pw, k.r1inv);
         else
-          pw = ff_pow(k.r1, L);
-        Lp = L;
+          pw = ff_pow(k.r1, e);
+        Lp = e;
         pinit = true;
         const FF p2 = ff_mul(pw, pw);
         ph[0] = F2{p2.h, p2.h};
@@ -994,23 +973,29 @@ TCW_HD void exp_column2(const float *__restrict__ atoms8, const Geom &g,
 #pragma unroll
         for (int c = 0; c < 2; c++) nph[c] = F2{-ph[c].x, -ph[c].y};
       }
-      FF2 W[4];
+      F2 x[4];
+      TCW_DCHECK(wtop < g.numAtoms);
+      load_row8(atoms8 + (size_t)wtop * 8u, x);
 #pragma unroll
       for (int c = 0; c < 4; c++)
-        W[c] = ff2_sub_scaled_fast(Elo[c], ph[c >> 1], nph[c >> 1], pl[c >> 1], Ehi[c]);
-      const F2 s0 = add2(W[0].h, W[0].l), s1 = add2(W[1].h, W[1].l);
-      const F2 s2 = add2(W[2].h, W[2].l), s3 = add2(W[3].h, W[3].l);
-      if (fstat_fast_sums(s0.x, s0.y, s1.x, s2.x, s2.y, s3.x, s3.y, F)) {
-        ok = true;
-      } else {
-#pragma unroll
-        for (int c = 0; c < 4; c++)
-          W[c] = ff2_sub_scaled_exact(Elo[c], ph[c >> 1], nph[c >> 1], pl[c >> 1], Ehi[c]);
-        FF Ws[7];
-        ff2_unpack_row8(W, Ws);
-        F = fstat_ff<kFp64Det>(Ws[0], Ws[1], Ws[2], Ws[3], Ws[4], Ws[5], Ws[6], ok);
-      }
+        W[c] = ff2_sub_scaled_x(W[c], ph[c >> 1], nph[c >> 1], pl[c >> 1], x[c]);
     }
+    while (wlo > lo) {
+      wlo--;
+      F2 x[4];
+      TCW_DCHECK(wlo < g.numAtoms);
+      load_row8(atoms8 + (size_t)wlo * 8u, x);
+#pragma unroll
+      for (int c = 0; c < 4; c++)
+        W[c] = ff2_axpy(x[c], k2.rh[c >> 1], k2.nrh[c >> 1], k2.rl[c >> 1], W[c]);
+      if (x[0].x != 0.0f || x[0].y != 0.0f) nz = wlo;
+    }
+    if (nz > hi) {  // no data in the window: zero sums, cond = inf
+      sink(m, 2.0f, false);
+      continue;
+    }
+    bool ok;
+    const float F = fstat_tiered_row8<kFp64Det>(W, ok);
     sink(m, F, ok);
   }
 }

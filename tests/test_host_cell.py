@@ -129,3 +129,21 @@ def test_random_gappy_grids(hostcell, oracle):
             Fr = port(A, 1800, t0_data, t0s, taus)
             clear = (cond > 1.01e4) | ~np.isfinite(cond)
             assert np.all(F[clear] == 2.0) and np.all(Fr[clear] == 2.0), (seed, window)
+
+
+@pytest.mark.parametrize("dt0", [667, 1800, 4861])
+def test_exp_long_columns_many_removals(hostcell, oracle, dt0):
+    """Long exponential columns: the sliding window sum adds and removes
+    thousands of atoms per column (short taus remove one or more atoms on
+    almost every row, long ones clamp at the data end) and stays within the
+    tolerance of FP64 on every cell."""
+    t0_data, A = synth.merged_atoms(31, 1500, 2, gap_frac=0.1)
+    span = A.shape[0] * 1800
+    nt0 = min(700, span // dt0)
+    t0s = (t0_data - 900 + np.arange(nt0) * dt0).astype(np.uint32)
+    taus = np.unique(np.round(1800 * np.logspace(0, np.log10(span / 1800), 40))).astype(np.uint32)
+    c = dict(window=2, atoms=A, TAtom=1800, t0_data=t0_data, t0s=t0s, taus=taus)
+    F64, cond = oracle.map_f64(A, 1800, t0_data, 2, t0s, taus, with_cond=True)
+    F, _ = hc_map(hostcell, c)
+    rel, _ = rel_err(F, F64, cond)
+    assert rel.max() < REL_TOL, rel.max()
