@@ -454,7 +454,7 @@ __device__ void exp_tile(const TemplateDev &t, const WorkItem &w, const float *_
 #define TCW_RECT_MIN_BLOCKS 5
 #endif
 #ifndef TCW_EXP_MIN_BLOCKS
-#define TCW_EXP_MIN_BLOCKS 6
+#define TCW_EXP_MIN_BLOCKS 8
 #endif
 
 template <int kWin, bool kPersist, bool kWrite, int kPrec>
