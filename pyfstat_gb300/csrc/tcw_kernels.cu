@@ -291,18 +291,19 @@ __device__ void block_reduce_store(const Red &red, Partial *out) {
 // columns, so the row's start index, its prefix row and the u32-wrap state
 // are set up once per row; per cell only the end index and one prefix row
 // are needed, and the next cell's prefix row is loaded while the current
-// cell is computed.  The block's 4 warps are (rg row groups of 32 rows) x
-// (4/rg column ranges).  With a map to write, each warp transposes 32 x 32
-// blocks through shared memory so that global stores are row-contiguous.
+// cell is computed.  A call covers the 32 rows of row group my_rg and
+// column range my_cg of cgs equal ranges: one-tile-per-block launches give
+// the block's 4 warps (rg row groups) x (4/rg column ranges), persistent
+// launches give one warp all row groups in turn with cgs = 1.  With a map to
+// write, each warp transposes 32 x 32 blocks through shared memory so that
+// global stores are row-contiguous.
 template <bool kWrite, int kPrec>
 __device__ void rect_tile(const TemplateDev &t, const WorkItem &w,
                           const uint32_t *__restrict__ t0s_all,
                           const uint32_t *__restrict__ taus_all, const float *__restrict__ P_all,
-                          float *__restrict__ Fmn, Red &red, float *smw) {
-  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-  const uint32_t rg = w.tn;  // row groups: 1, 2 or 4
-  const uint32_t cgs = 4u / rg;
-  const uint32_t my_rg = warp % rg, my_cg = warp / rg;
+                          float *__restrict__ Fmn, Red &red, float *smw, uint32_t my_rg,
+                          uint32_t cgs, uint32_t my_cg) {
+  const uint32_t lane = threadIdx.x & 31u;
   const uint32_t mbase = w.m0 + 32u * my_rg;
   const uint32_t m = mbase + lane;
   const bool row_ok = m < w.m1;
@@ -470,6 +471,40 @@ __global__ void __launch_bounds__(kBlock, kWin == TCW_WINDOW_RECT ? TCW_RECT_MIN
   constexpr uint32_t kSmem = kWin == TCW_WINDOW_RECT ? (kWrite ? (kBlock / 32) * 32 * 33 : 1)
                                                      : kExpLoTab;
   __shared__ __align__(16) uint32_t sm[kSmem];
+  if (kWin == TCW_WINDOW_RECT && kPersist) {
+    // Persistent rectangular launches schedule by warp: each warp fetches
+    // whole tiles and walks their 32-row groups in turn, merging the groups'
+    // reducers in row order, so no block barrier waits on the slowest warp
+    // (rect warps share no shared memory).
+    const uint32_t lane = threadIdx.x & 31u;
+    float *smw = reinterpret_cast<float *>(sm) + (threadIdx.x >> 5) * (32 * 33);
+    for (;;) {
+      uint32_t it2 = 0;
+      if (lane == 0) it2 = atomicAdd(counter, 1u);
+      it2 = __shfl_sync(0xffffffffu, it2, 0);
+      if (it2 >= n_items) break;
+      const WorkItem w = items[it2];
+      const TemplateDev t = T[w.tmpl];
+      RedVal acc{-INFINITY, INT64_MAX, 0.0f};
+      for (uint32_t g = 0; g < w.tn; g++) {
+        Red red;
+        red.init();
+        rect_tile<kWrite, kPrec>(t, w, t0s, taus, P, Fmn, red, smw, g, 1u, 0u);
+        acc = red_combine(acc, RedVal{red.mx, red.bidx, fsub(red.s, red.c)});
+      }
+#pragma unroll
+      for (int d = 16; d > 0; d >>= 1) acc = red_combine(acc, shfl_down_red(acc, d));
+      if (lane == 0) {
+        Partial pp;
+        pp.maxF = acc.mx;
+        pp.pad = 0;
+        pp.argmax = acc.bidx;
+        pp.s = (acc.mx == -INFINITY) ? 0.0 : (double)acc.s;
+        parts[w.part] = pp;
+      }
+    }
+    return;
+  }
   uint32_t it = blockIdx.x;
   for (;;) {
     if (kPersist) {
@@ -483,10 +518,12 @@ __global__ void __launch_bounds__(kBlock, kWin == TCW_WINDOW_RECT ? TCW_RECT_MIN
     const TemplateDev t = T[w.tmpl];
     Red red;
     red.init();
-    if (kWin == TCW_WINDOW_RECT)
+    if (kWin == TCW_WINDOW_RECT) {
+      const uint32_t warp = threadIdx.x >> 5, rg = w.tn;
       rect_tile<kWrite, kPrec>(t, w, t0s, taus, P, Fmn, red,
-                               reinterpret_cast<float *>(sm) + (threadIdx.x >> 5) * (32 * 33));
-    else
+                               reinterpret_cast<float *>(sm) + warp * (32 * 33), warp % rg,
+                               4u / rg, warp / rg);
+    } else
       exp_tile<kWrite, kPrec>(t, w, atoms, atoms8, t0s, taus, Fmn, red, sm);
     block_reduce_store(red, parts + w.part);
     if (!kPersist) break;
