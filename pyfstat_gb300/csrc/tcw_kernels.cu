@@ -454,13 +454,25 @@ __device__ void exp_tile(const TemplateDev &t, const WorkItem &w, const float *_
 #ifndef TCW_RECT_MIN_BLOCKS
 #define TCW_RECT_MIN_BLOCKS 5
 #endif
+// The persistent map-less exp kernel (the batched plans' hot kernel) runs
+// fastest at 8 blocks (64 registers, a few spilled); the exp kernels that
+// write maps or run one tile per block keep 96 registers without spills.
 #ifndef TCW_EXP_MIN_BLOCKS
 #define TCW_EXP_MIN_BLOCKS 8
 #endif
+#ifndef TCW_EXP_MIN_BLOCKS_OTHER
+#define TCW_EXP_MIN_BLOCKS_OTHER 5
+#endif
+
+template <int kWin, bool kPersist, bool kWrite>
+constexpr int map_min_blocks() {
+  return kWin == TCW_WINDOW_RECT ? TCW_RECT_MIN_BLOCKS
+         : (kPersist && !kWrite) ? TCW_EXP_MIN_BLOCKS
+                                 : TCW_EXP_MIN_BLOCKS_OTHER;
+}
 
 template <int kWin, bool kPersist, bool kWrite, int kPrec>
-__global__ void __launch_bounds__(kBlock, kWin == TCW_WINDOW_RECT ? TCW_RECT_MIN_BLOCKS
-                                                                  : TCW_EXP_MIN_BLOCKS)
+__global__ void __launch_bounds__(kBlock, (map_min_blocks<kWin, kPersist, kWrite>()))
     map_kernel(const TemplateDev *__restrict__ T, const WorkItem *__restrict__ items,
                uint32_t n_items, uint32_t *__restrict__ counter, const float *__restrict__ atoms,
                const float *__restrict__ atoms8, const uint32_t *__restrict__ t0s,
