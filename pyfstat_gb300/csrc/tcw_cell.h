@@ -455,15 +455,19 @@ TCW_HD float fstat_ff(FF A, FF B, FF C, FF Far, FF Fai, FF Fbr, FF Fbi, bool &ok
 // bounds A B / D), and F = |G|^2/(B D) + |Fb|^2/B with G = B Fa - C Fb adds
 // <= 2 eps (1 + sqrt(cond)/2): about 1.5e-6 in all.  Returns false (and no
 // F) when the cell needs tier 2 (fstat_ff on the double-word sums).
+//
+// The selection needs no square root: with S = A + B > 0 and D > 0 the
+// eigenvalues of [[A, C], [C, B]] are (S +- sqrt(S^2 - 4D))/2, and
+// cond < K  <=>  sqrt(S^2 - 4D) (1 + K) < S (K - 1)  <=>  K S^2 < (1 + K)^2 D.
+// A cell with D <= 0 (or a NaN) fails the test and goes to tier 2.
 constexpr float kFastCond = 32.0f;
+constexpr float kFastCondRhs = (1.0f + kFastCond) * (1.0f + kFastCond);
 
 TCW_HD bool fstat_fast_sums(float A, float B, float C, float Far, float Fai, float Fbr,
                             float Fbi, float &F) {
   const float D = ffma(A, B, -fmul(C, C));
-  const float dAB = fsub(A, B);
-  const float disc = sqrt_approx(ffma(dAB, dAB, fmul(4.0f * C, C)));
-  const float t = fadd(fadd(A, B), disc);
-  if (!(fmul(t, t) < fmul(4.0f * kFastCond, D))) return false;
+  const float S = fadd(A, B);
+  if (!(fmul(fmul(kFastCond, S), S) < fmul(kFastCondRhs, D))) return false;
   const float Gre = ffma(B, Far, -fmul(C, Fbr));
   const float Gim = ffma(B, Fai, -fmul(C, Fbi));
   const float num = ffma(D, ffma(Fbr, Fbr, fmul(Fbi, Fbi)), ffma(Gre, Gre, fmul(Gim, Gim)));
