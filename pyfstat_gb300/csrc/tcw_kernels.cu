@@ -294,15 +294,18 @@ __device__ void block_reduce_store(const Red &red, Partial *out) {
 // cell is computed.  A call covers the 32 rows of row group my_rg and
 // column range my_cg of cgs equal ranges: one-tile-per-block launches give
 // the block's 4 warps (rg row groups) x (4/rg column ranges), persistent
-// launches give one warp all row groups in turn with cgs = 1.  With a map to
-// write, each warp transposes 32 x 32 blocks through shared memory so that
-// global stores are row-contiguous.
+// launches give one warp all row groups in turn with cgs = 1.  The columns'
+// taus are staged 32 at a time in the warp's `stau` slots of shared memory
+// (one coalesced load per 32 columns instead of a global load on every
+// cell's end-index chain).  With a map to write, each warp transposes
+// 32 x 32 blocks through shared memory so that global stores are
+// row-contiguous.
 template <bool kWrite, int kPrec>
 __device__ void rect_tile(const TemplateDev &t, const WorkItem &w,
                           const uint32_t *__restrict__ t0s_all,
                           const uint32_t *__restrict__ taus_all, const float *__restrict__ P_all,
                           float *__restrict__ Fmn, Red &red, float *smw, uint32_t my_rg,
-                          uint32_t cgs, uint32_t my_cg) {
+                          uint32_t cgs, uint32_t my_cg, uint32_t *stau) {
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t mbase = w.m0 + 32u * my_rg;
   const uint32_t m = mbase + lane;
@@ -325,8 +328,8 @@ __device__ void rect_tile(const TemplateDev &t, const WorkItem &w,
     TCW_DCHECK(j0 <= t.g.numAtoms);
     ld_row16(P + (size_t)j0 * kPrefixStride, row0);
   }
-  auto end_of = [&](uint32_t n) {
-    uint32_t e = idx_end(t0 + __ldg(taus + n), t.g);
+  auto end_of = [&](uint32_t tau) {
+    uint32_t e = idx_end(t0 + tau, t.g);
     return (wr && ef > e) ? ef : e;
   };
   const int64_t rowidx = (int64_t)m * t.N_tau;
@@ -334,7 +337,7 @@ __device__ void rect_tile(const TemplateDev &t, const WorkItem &w,
   uint32_t e_cur = 0;
   float cur[16], nxt[16];
   if (row_ok && nb < ne) {
-    e_cur = end_of(nb);
+    e_cur = end_of(__ldg(taus + nb));
     TCW_DCHECK(e_cur + 1u <= t.g.numAtoms);
     ld_row16(P + (size_t)(e_cur + 1u) * kPrefixStride, cur);
   }
@@ -343,7 +346,7 @@ __device__ void rect_tile(const TemplateDev &t, const WorkItem &w,
   auto cell = [&](uint32_t n, uint32_t cb, const float *a, uint32_t ea, float *b,
                   uint32_t &eb) {
     if (row_ok && n + 1u < ne) {
-      eb = end_of(n + 1u);
+      eb = end_of(n + 1u < cb + 32u ? stau[n + 1u - cb] : __ldg(taus + n + 1u));
       TCW_DCHECK(eb + 1u <= t.g.numAtoms);
       ld_row16(P + (size_t)(eb + 1u) * kPrefixStride, b);
     }
@@ -371,6 +374,9 @@ __device__ void rect_tile(const TemplateDev &t, const WorkItem &w,
   };
   for (uint32_t cb = nb; cb < ne; cb += 32u) {
     const uint32_t ce = min(ne, cb + 32u);
+    __syncwarp();
+    if (cb + lane < ne) stau[lane] = __ldg(taus + cb + lane);
+    __syncwarp();
     // ping-pong between the two row buffers; `cur` holds column n on entry
     uint32_t n = cb;
     for (; n + 1u < ce; n += 2u) {
@@ -483,6 +489,7 @@ __global__ void __launch_bounds__(kBlock, (map_min_blocks<kWin, kPersist, kWrite
   constexpr uint32_t kSmem = kWin == TCW_WINDOW_RECT ? (kWrite ? (kBlock / 32) * 32 * 33 : 1)
                                                      : kExpLoTab;
   __shared__ __align__(16) uint32_t sm[kSmem];
+  __shared__ uint32_t s_tau[kWin == TCW_WINDOW_RECT ? kBlock : 1];
   if (kWin == TCW_WINDOW_RECT && kPersist) {
     // Persistent rectangular launches schedule by warp: each warp fetches
     // whole tiles and walks their 32-row groups in turn, merging the groups'
@@ -501,7 +508,8 @@ __global__ void __launch_bounds__(kBlock, (map_min_blocks<kWin, kPersist, kWrite
       for (uint32_t g = 0; g < w.tn; g++) {
         Red red;
         red.init();
-        rect_tile<kWrite, kPrec>(t, w, t0s, taus, P, Fmn, red, smw, g, 1u, 0u);
+        rect_tile<kWrite, kPrec>(t, w, t0s, taus, P, Fmn, red, smw, g, 1u, 0u,
+                                 s_tau + (threadIdx.x >> 5) * 32u);
         acc = red_combine(acc, RedVal{red.mx, red.bidx, fsub(red.s, red.c)});
       }
 #pragma unroll
@@ -534,7 +542,7 @@ __global__ void __launch_bounds__(kBlock, (map_min_blocks<kWin, kPersist, kWrite
       const uint32_t warp = threadIdx.x >> 5, rg = w.tn;
       rect_tile<kWrite, kPrec>(t, w, t0s, taus, P, Fmn, red,
                                reinterpret_cast<float *>(sm) + warp * (32 * 33), warp % rg,
-                               4u / rg, warp / rg);
+                               4u / rg, warp / rg, s_tau + warp * 32u);
     } else
       exp_tile<kWrite, kPrec>(t, w, atoms, atoms8, t0s, taus, Fmn, red, sm);
     block_reduce_store(red, parts + w.part);
