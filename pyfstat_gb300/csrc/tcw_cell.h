@@ -508,36 +508,13 @@ TCW_HD float fstat_tiered2(const FF2 P[4], bool &ok) {
   return fstat_ff<kFp64Det>(W[0], W[1], W[2], W[3], W[4], W[5], W[6], ok);
 }
 
-// Exponential columns pair the channels by decay ratio instead: (A,B) and
-// (C,-) decay with r^2, (Fa_re,Fa_im) and (Fb_re,Fb_im) with r, so each
-// packed pair has one ratio in both lanes.  Atom rows of 8 floats hold the
-// channels in that order: [a2 b2 ab 0 Fa_re Fa_im Fb_re Fb_im]; kRow8Slot[c]
-// is the slot of channel c (a2 b2 ab Fa_re Fa_im Fb_re Fb_im).
+// Exponential columns hold the channels by decay ratio: (A,B) as a packed
+// pair and C as a scalar double-word decay with r^2, (Fa_re,Fa_im) and
+// (Fb_re,Fb_im) as packed pairs with r, so each packed pair has one ratio in
+// both lanes.  Atom rows of 8 floats hold the channels in that order:
+// [a2 b2 ab 0 Fa_re Fa_im Fb_re Fb_im]; kRow8Slot[c] is the slot of channel c
+// (a2 b2 ab Fa_re Fa_im Fb_re Fb_im).
 constexpr int kRow8Slot[7] = {0, 1, 2, 4, 5, 6, 7};
-
-TCW_HD void ff2_unpack_row8(const FF2 P[4], FF W[7]) {
-  W[0] = FF{P[0].h.x, P[0].l.x};
-  W[1] = FF{P[0].h.y, P[0].l.y};
-  W[2] = FF{P[1].h.x, P[1].l.x};
-  W[3] = FF{P[2].h.x, P[2].l.x};
-  W[4] = FF{P[2].h.y, P[2].l.y};
-  W[5] = FF{P[3].h.x, P[3].l.x};
-  W[6] = FF{P[3].h.y, P[3].l.y};
-}
-
-template <bool kFp64Det>
-TCW_HD float fstat_tiered_row8(const FF2 P[4], bool &ok) {
-  const F2 s0 = add2(P[0].h, P[0].l), s1 = add2(P[1].h, P[1].l);
-  const F2 s2 = add2(P[2].h, P[2].l), s3 = add2(P[3].h, P[3].l);
-  float F;
-  if (fstat_fast_sums(s0.x, s0.y, s1.x, s2.x, s2.y, s3.x, s3.y, F)) {
-    ok = true;
-    return F;
-  }
-  FF W[7];
-  ff2_unpack_row8(P, W);
-  return fstat_ff<kFp64Det>(W[0], W[1], W[2], W[3], W[4], W[5], W[6], ok);
-}
 
 // Both tiers for double-word window sums that are exact enough for tier 2.
 template <bool kFp64Det>
@@ -863,12 +840,13 @@ TCW_HD void exp_column(const float *__restrict__ atoms, const Geom &g,
 }
 
 // ------------------------------------------------------------ packed exponential column
-// The same column walk as exp_column with the seven channels in four packed
-// pairs and the atoms in 32-byte rows [a2 b2 ab 0 Fa_re Fa_im Fb_re Fb_im]
-// (one 256-bit load per recurrence step on the device).  Pairs 0 and 1 of
-// the state run with the ratio r^2 in both lanes, pairs 2 and 3 with r, so
-// the per-column constants are two packed ratios (and two packed tail
-// factors) rather than four.
+// The same windows as exp_column with the atoms in 32-byte rows
+// [a2 b2 ab 0 Fa_re Fa_im Fb_re Fb_im] (one 256-bit load per step on the
+// device) and the channels as three packed pairs (A,B) with r^2, (Fa) and
+// (Fb) with r, plus C as a scalar double-word with r^2: one ratio per pair,
+// so the per-column constants are two packed ratios and two packed tail
+// factors, and C does not spend a packed operation (two FMA-pipe cycles) on
+// an idle lane.
 TCW_HD void load_row8(const float *__restrict__ p, F2 x[4]) {
 #if defined(__CUDA_ARCH__)
   asm volatile("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
@@ -880,7 +858,7 @@ TCW_HD void load_row8(const float *__restrict__ p, F2 x[4]) {
 #endif
 }
 
-// Index 0: r^2 (pairs 0, 1); index 1: r (pairs 2, 3).
+// Index 0: r^2 (the (A,B) pair); index 1: r (the Fa and Fb pairs).
 struct ExpConsts2 {
   F2 rh[2], nrh[2], rl[2];
 };
@@ -910,6 +888,16 @@ TCW_HD FF2 ff2_sub_scaled_x(FF2 W, F2 ph, F2 nph, F2 pl, F2 x) {
   return FF2{s, sub2(add2(e, W.l), ae)};
 }
 
+// The scalar form of ff2_sub_scaled_x (W - p*x for the C channel).
+TCW_HD FF ff_sub_scaled_x1(FF W, FF p, float x) {
+  const float a = fmul(p.h, x);
+  float ae = ffma(p.h, x, -a);
+  ae = ffma(p.l, x, ae);
+  float sh, se;
+  two_sum(W.h, -a, sh, se);
+  return FF{sh, fsub(fadd(se, W.l), ae)};
+}
+
 // One sliding window sum per column.  W holds, for the atom range
 // [wlo, wtop), sum_i x_i r^(i - wlo) (r^2 for A, B, C): the common factor
 // e^(-k (t_wlo - t0)/tau) of the exponential weights is dropped as in
@@ -929,15 +917,14 @@ TCW_HD void exp_column2(const float *__restrict__ atoms8, const Geom &g,
                         uint32_t tau, Sink &sink, const uint32_t *lo_tab = nullptr) {
   const ExpConsts k = exp_consts(g.TAtom, tau);
   const ExpConsts2 k2 = exp_consts2(k);
-  FF2 W[4];
   const F2 z{0.0f, 0.0f};
-#pragma unroll
-  for (int c = 0; c < 4; c++) W[c] = FF2{z, z};
-  uint32_t wlo = 0, wtop = 0;
-  uint32_t nz = 0xFFFFFFFFu;  // lowest atom >= wlo with a2 or b2 non-zero
-  uint32_t Lp = 0;            // exponent of the cached power pw = r^Lp
-  FF pw{1.0f, 0.0f};
-  F2 ph[2], nph[2], pl[2];    // r^(2 Lp) and r^Lp, packed
+  FF2 W0{z, z}, W2{z, z}, W3{z, z};  // (A,B), (Fa_re,Fa_im), (Fb_re,Fb_im)
+  FF Wc{0.0f, 0.0f};                 // C
+  uint32_t wlo = 0, wtop = 0;        // W holds the window [wlo, wtop)
+  uint32_t nz = 0xFFFFFFFFu;         // lowest atom >= wlo with a2 or b2 non-zero
+  uint32_t Lp = 0;                   // exponent of the cached powers pw = r^Lp, p2 = r^(2 Lp)
+  FF pw{1.0f, 0.0f}, p2{1.0f, 0.0f};
+  F2 ph[2], nph[2], pl[2];           // p2 and pw, packed
   bool pinit = false;
   bool init = false;
   for (uint32_t mm = m_end; mm > m_begin; mm--) {
@@ -953,8 +940,8 @@ TCW_HD void exp_column2(const float *__restrict__ atoms8, const Geom &g,
     if (!init || top > wtop || lo > wlo || top <= wlo) {
       wlo = wtop = top;
       nz = 0xFFFFFFFFu;
-#pragma unroll
-      for (int c = 0; c < 4; c++) W[c] = FF2{z, z};
+      W0 = W2 = W3 = FF2{z, z};
+      Wc = FF{0.0f, 0.0f};
       init = true;
     }
     while (wtop > top) {
@@ -969,7 +956,7 @@ TCW_HD void exp_column2(const float *__restrict__ atoms8, const Geom &g,
           pw = ff_pow(k.r1, e);
         Lp = e;
         pinit = true;
-        const FF p2 = ff_mul(pw, pw);
+        p2 = ff_mul(pw, pw);
         ph[0] = F2{p2.h, p2.h};
         pl[0] = F2{p2.l, p2.l};
         ph[1] = F2{pw.h, pw.h};
@@ -980,26 +967,35 @@ TCW_HD void exp_column2(const float *__restrict__ atoms8, const Geom &g,
       F2 x[4];
       TCW_DCHECK(wtop < g.numAtoms);
       load_row8(atoms8 + (size_t)wtop * 8u, x);
-#pragma unroll
-      for (int c = 0; c < 4; c++)
-        W[c] = ff2_sub_scaled_x(W[c], ph[c >> 1], nph[c >> 1], pl[c >> 1], x[c]);
+      W0 = ff2_sub_scaled_x(W0, ph[0], nph[0], pl[0], x[0]);
+      Wc = ff_sub_scaled_x1(Wc, p2, x[1].x);
+      W2 = ff2_sub_scaled_x(W2, ph[1], nph[1], pl[1], x[2]);
+      W3 = ff2_sub_scaled_x(W3, ph[1], nph[1], pl[1], x[3]);
     }
     while (wlo > lo) {
       wlo--;
       F2 x[4];
       TCW_DCHECK(wlo < g.numAtoms);
       load_row8(atoms8 + (size_t)wlo * 8u, x);
-#pragma unroll
-      for (int c = 0; c < 4; c++)
-        W[c] = ff2_axpy(x[c], k2.rh[c >> 1], k2.nrh[c >> 1], k2.rl[c >> 1], W[c]);
+      W0 = ff2_axpy(x[0], k2.rh[0], k2.nrh[0], k2.rl[0], W0);
+      Wc = ff_axpy(x[1].x, k.r2, Wc);
+      W2 = ff2_axpy(x[2], k2.rh[1], k2.nrh[1], k2.rl[1], W2);
+      W3 = ff2_axpy(x[3], k2.rh[1], k2.nrh[1], k2.rl[1], W3);
       if (x[0].x != 0.0f || x[0].y != 0.0f) nz = wlo;
     }
     if (nz > hi) {  // no data in the window: zero sums, cond = inf
       sink(m, 2.0f, false);
       continue;
     }
-    bool ok;
-    const float F = fstat_tiered_row8<kFp64Det>(W, ok);
+    // tier 1 from the rounded sums, tier 2 from the double-words
+    bool ok = true;
+    float F;
+    const F2 s0 = add2(W0.h, W0.l), s2 = add2(W2.h, W2.l), s3 = add2(W3.h, W3.l);
+    const float sc = fadd(Wc.h, Wc.l);
+    if (!fstat_fast_sums(s0.x, s0.y, sc, s2.x, s2.y, s3.x, s3.y, F)) {
+      F = fstat_ff<kFp64Det>(FF{W0.h.x, W0.l.x}, FF{W0.h.y, W0.l.y}, Wc, FF{W2.h.x, W2.l.x},
+                             FF{W2.h.y, W2.l.y}, FF{W3.h.x, W3.l.x}, FF{W3.h.y, W3.l.y}, ok);
+    }
     sink(m, F, ok);
   }
 }
