@@ -277,8 +277,11 @@ def profile_figure(kernel, key):
 
 def roofline_block(batch, rect_ms, exp_ms, prefix_ms, fin_ms, peaks, clk, n_sms):
     """Roofline of the dominant map kernel: cells/s against the minimum over
-    {FP32, MUFU, FP64, HBM} of measured peak / per-cell algorithmic demand;
-    with the FP32-flop view and the instruction-issue view of the same kernel."""
+    {FP32, MUFU, FP64, HBM} of measured peak / per-cell algorithmic demand,
+    stated in the binding unit (algorithmic TFLOP/s or GB/s per second of
+    kernel time against that unit's measured peak; the fraction is the same
+    in cells/s); with the FP32-flop view and the instruction-issue view of
+    the same kernel."""
     hbm = None
     try:
         with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
@@ -303,7 +306,15 @@ def roofline_block(batch, rect_ms, exp_ms, prefix_ms, fin_ms, peaks, clk, n_sms)
             bounds["hbm"] = hbm * 1e9 / (nbytes / cells)
         bound = min(bounds, key=bounds.get)
         cps = cells / (ms * 1e-3)
+        # the binding unit's algorithmic work per second against its peak
+        if bound == "hbm":
+            unit, ach, pk = "GB/s", cps * (nbytes / cells) / 1e9, hbm
+        elif bound == "mufu":
+            unit, ach, pk = "Tops/s", cps * d["mufu"] / 1e12, peaks["mufu_tops"]
+        else:
+            unit, ach, pk = "TFLOP/s", cps * d[bound] / 1e12, peaks[f"{bound}_tflops"]
         k = {"ms": ms, "cells": cells, "cells_per_s": cps, "bound": bound,
+             "bound_unit": unit, "achieved": ach, "peak": pk,
              "roofline_cells_per_s": bounds[bound], "frac": cps / bounds[bound],
              "unit_bounds_cells_per_s": bounds, "algorithmic_per_cell": d,
              "algorithmic_bytes_per_launch": nbytes,
@@ -318,8 +329,9 @@ def roofline_block(batch, rect_ms, exp_ms, prefix_ms, fin_ms, peaks, clk, n_sms)
         kernels[name] = k
     dom = max(kernels, key=lambda n: kernels[n]["ms"])
     d = kernels[dom]
-    return {"bound": d["bound"], "achieved": d["cells_per_s"], "peak": d["roofline_cells_per_s"],
-            "unit": "cells/s", "frac": d["frac"], "traffic": traffic_per_launch(dom),
+    return {"bound": d["bound"], "achieved": d["achieved"], "peak": d["peak"],
+            "unit": d["bound_unit"], "frac": d["frac"], "traffic": traffic_per_launch(dom),
+            "achieved_cells_per_s": d["cells_per_s"], "roofline_cells_per_s": d["roofline_cells_per_s"],
             "kernel": dom, "kernels": kernels, "prefix_ms": prefix_ms, "finalize_ms": fin_ms,
             "peak_source": "FP32/FP64/MUFU of measured (tcw_probe_peaks on this GPU), HBM of "
                            "measured (MEASURED_PEAKS.json)",
