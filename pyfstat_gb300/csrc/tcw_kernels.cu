@@ -460,9 +460,11 @@ __device__ void exp_tile(const TemplateDev &t, const WorkItem &w, const float *_
 #ifndef TCW_RECT_MIN_BLOCKS
 #define TCW_RECT_MIN_BLOCKS 5
 #endif
-// The persistent map-less exp kernel (the batched plans' hot kernel) runs
-// fastest at 8 blocks (64 registers, a few spilled); the exp kernels that
-// write maps or run one tile per block keep 96 registers without spills.
+// The persistent exp kernels (the batched plans' hot kernels, with or
+// without maps) run fastest at 8 blocks (64 registers, a few spilled); the
+// one-tile-per-block exp kernels of single-template calls keep 96 registers
+// without spills (their grids are small, so latency matters more than
+// occupancy).
 #ifndef TCW_EXP_MIN_BLOCKS
 #define TCW_EXP_MIN_BLOCKS 8
 #endif
@@ -473,7 +475,7 @@ __device__ void exp_tile(const TemplateDev &t, const WorkItem &w, const float *_
 template <int kWin, bool kPersist, bool kWrite>
 constexpr int map_min_blocks() {
   return kWin == TCW_WINDOW_RECT ? TCW_RECT_MIN_BLOCKS
-         : (kPersist && !kWrite) ? TCW_EXP_MIN_BLOCKS
+         : kPersist ? TCW_EXP_MIN_BLOCKS
                                  : TCW_EXP_MIN_BLOCKS_OTHER;
 }
 
