@@ -1,0 +1,66 @@
+"""The benchmark's one-line JSON output: the reference arm on the CPU (the
+oracle port of the reference's CPU path) and, on a GPU, this library's arm
+on a small batch.  Checks the keys and types the line promises, not the
+numbers."""
+
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def run_bench(*args, timeout=600):
+    r = subprocess.run([sys.executable, os.path.join(REPO, "bench.py"), *args], cwd=REPO,
+                       capture_output=True, text=True, timeout=timeout)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1, r.stdout[-2000:]
+    return json.loads(lines[0])
+
+
+def check_common(d, steps, warmup):
+    assert d["metric"] and d["unit"] == "cells/s"
+    assert d["value"] > 0 and d["ms_per_step"] > 0
+    assert d["n_gpus"] == 1 and d["steps"] == steps and d["warmup"] == warmup
+    assert d["higher_is_better"] is True and d["scaling"] == "weak"
+    assert d["vs_baseline"] is None
+    assert d["dtype"] == "f32" and d["data"] == "synthetic"
+    assert isinstance(d["config"]["workload"], str)
+
+
+def test_reference_arm_line():
+    d = run_bench("--impl", "reference", "--steps", "1", "--warmup", "0", "--templates", "8",
+                  "--cpu-seconds", "0.5")
+    check_common(d, 1, 0)
+    assert d["impl"] == "reference"
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] and cb["unit"] == "cells/s"
+    assert cb["cores"] >= 1 and cb["kind"] in ("port", "reference") and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": "cells/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
+
+
+@pytest.mark.gpu
+def test_gpu_arm_line():
+    d = run_bench("--steps", "2", "--warmup", "3", "--templates", "64", "--plain-templates", "4",
+                  "--cpu-seconds", "0.5", "--tile", "default")
+    check_common(d, 2, 3)
+    assert "impl" not in d or d["impl"] == "ours"
+    r = d["roofline"]
+    assert r["bound"] in ("fp64", "fp32", "mufu", "hbm")
+    assert r["unit"] in ("TFLOP/s", "GB/s", "Tops/s")
+    assert 0 < r["achieved"] and 0 < r["peak"]
+    assert r["frac"] == pytest.approx(r["achieved"] / r["peak"], rel=1e-9)
+    assert r["traffic"] is None or r["traffic"] > 0
+    cb = d["cpu_baseline"]
+    assert cb["value"] > 0 and cb["cores"] >= 1 and cb["kind"] == "port"
+    e = d["e2e"]
+    assert e["value"] > 0 and e["unit"] == "cells/s"
+    assert e["h2d_bytes_per_step"] > 0 and e["d2h_bytes_per_step"] > 0
+    assert d["gpu_launches"] >= 2 * 5
+    c = d["clocks"]
+    assert "sm_mhz" in c and "sm_max_mhz" in c and isinstance(c["reasons"], list)
