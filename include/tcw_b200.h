@@ -115,6 +115,11 @@ int tcw_destroy(tcw_handle *h);
 int tcw_get_stream(tcw_handle *h, void **stream);
 int tcw_set_stream(tcw_handle *h, void *stream);
 int tcw_sync(tcw_handle *h, int timeout_ms);     /* TCW_ERR_TIMEOUT if not done in time */
+/* Page-locked host memory (cudaHostAlloc / cudaFreeHost) for the asynchronous
+ * host-buffer entry points: copies from or into pageable memory make the
+ * calling thread wait for the copy.  A helper with no reference counterpart. */
+int tcw_pinned_alloc(void **ptr, size_t bytes);
+int tcw_pinned_free(void *ptr);
 
 /* Plain per-template map on device buffers.  d_Fmn may be NULL (no map is
  * written; TCW_FLAG_POSTERIORS then needs a map and is rejected).  d_result
@@ -151,6 +156,17 @@ int tcw_plan_info(const tcw_plan *plan, uint64_t *n_cells, uint32_t *n_items,
 int tcw_plan_run(tcw_handle *h, tcw_plan *plan, const float *d_atoms, tcw_result *d_results,
                  int use_graph);
 int tcw_plan_run_host(tcw_handle *h, tcw_plan *plan, const float *atoms, tcw_result *results);
+/* As tcw_plan_run_host without waiting: the upload of `atoms` runs on the
+ * handle's copy stream and starts once the previous pipelined run on this
+ * handle has read its atoms (after its prefix and repack kernels), so it
+ * overlaps that run's map kernels; the results are copied back on the
+ * handle's stream.  `atoms` must stay unchanged and `results` unread until
+ * tcw_sync(h, ...) returns.  Both should be page-locked (tcw_pinned_alloc):
+ * with pageable `results` the download makes the caller wait for the run,
+ * and nothing overlaps.  Not for plans created with TCW_FLAG_POSTERIORS.  A
+ * pipelining addition for streams of batches (no reference counterpart). */
+int tcw_plan_run_host_async(tcw_handle *h, tcw_plan *plan, const float *atoms,
+                            tcw_result *results);
 /* As tcw_plan_run, and also writes every template's FP32 map: template k's
  * (N_t0, N_tau) row-major map starts at d_maps + sum_{j<k} N_t0(j) N_tau(j)
  * (descriptor order; tcw_plan_info's n_cells floats in all).  Replaces the

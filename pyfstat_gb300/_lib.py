@@ -101,6 +101,9 @@ SIGNATURES = {
     "tcw_plan_run_maps": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, ctypes.c_int]),
     "tcw_plan_run_maps_host": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp]),
     "tcw_plan_run_host": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
+    "tcw_plan_run_host_async": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
+    "tcw_pinned_alloc": (ctypes.c_int, [ctypes.POINTER(_vp), ctypes.c_size_t]),
+    "tcw_pinned_free": (ctypes.c_int, [_vp]),
     "tcw_plan_run_timed": (ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.POINTER(ctypes.c_float)]),
     "tcw_debug_fail_alloc": (ctypes.c_int, [_vp, ctypes.c_int]),
     "tcw_map_plain_noalloc": (ctypes.c_int, [_vp, _vp, _c_u32, _c_u32, _c_u32, ctypes.c_int, _vp,
@@ -200,6 +203,37 @@ def _ptr(a):
     if isinstance(a, np.ndarray):
         return a.ctypes.data
     return a.data_ptr()  # torch tensor
+
+
+class _PinnedBlock:
+    """Owner of one page-locked host allocation (freed when collected)."""
+
+    def __init__(self, nbytes):
+        p = _vp()
+        check(load().tcw_pinned_alloc(ctypes.byref(p), int(nbytes)))
+        self.ptr = p.value
+
+    def __del__(self):
+        try:
+            if self.ptr:
+                load().tcw_pinned_free(self.ptr)
+                self.ptr = None
+        except Exception:
+            pass
+
+
+def pinned_empty(shape, dtype=np.float32):
+    """An uninitialised numpy array in page-locked host memory."""
+    dtype = np.dtype(dtype)
+    shape = (shape,) if np.isscalar(shape) else tuple(shape)
+    nbytes = int(np.prod(shape)) * dtype.itemsize
+    block = _PinnedBlock(nbytes)
+    buf = (ctypes.c_char * max(nbytes, 1)).from_address(block.ptr)
+    arr = np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
+    arr_owner = arr.view()
+    # keep the allocation alive as long as any view of it is
+    buf._tcw_block = block
+    return arr_owner
 
 
 class Handle:
@@ -380,6 +414,34 @@ class Plan:
         check(load().tcw_plan_run_host(self.handle.ptr, self._p, atoms7.ctypes.data,
                                        res.ctypes.data), self.handle.ptr)
         return res
+
+    def run_host_async(self, atoms7):
+        """Pipelined :meth:`run_host`: enqueues the upload, the run and the
+        download of the results into a page-locked slot of this plan, and
+        returns at once.  The atoms are kept alive until :meth:`wait`, which
+        returns the results of the runs enqueued since the last wait, in
+        order.  Pass page-locked atoms (:func:`pinned_empty`) for the upload
+        to overlap the previous run's map kernels."""
+        atoms7 = np.ascontiguousarray(atoms7, dtype=np.float32)
+        if atoms7.shape[0] < self.n_atom_rows:
+            raise ValueError("atoms array shorter than the plan's atom rows")
+        if not hasattr(self, "_inflight"):
+            self._inflight, self._slots = [], []
+        k = len(self._inflight)
+        if k == len(self._slots):
+            self._slots.append(pinned_empty(self.n_templates, RESULT_DTYPE))
+        slot = self._slots[k]
+        self._inflight.append(atoms7)
+        check(load().tcw_plan_run_host_async(self.handle.ptr, self._p, atoms7.ctypes.data,
+                                             slot.ctypes.data), self.handle.ptr)
+
+    def wait(self, timeout_ms=600000):
+        """Waits for the pipelined runs; their results (copies), in order."""
+        self.handle.sync(timeout_ms)
+        n = len(getattr(self, "_inflight", []))
+        out = [self._slots[k].copy() for k in range(n)]
+        self._inflight = []
+        return out
 
     def run_maps_host(self, atoms7):
         """Host atoms in; (results, maps) out, maps a flat float32 array of

@@ -88,6 +88,15 @@ class TransientMapBatch:
         """Host atoms in (default: the templates' own), per-template results out."""
         return self.plan.run_host(self.atoms if atoms is None else atoms)
 
+    def run_pipelined(self, atom_batches):
+        """One run per host atom array (same layout as the templates' own),
+        pipelined: each upload overlaps the previous run's map kernels
+        (pinned arrays make the copies asynchronous).  Returns the
+        per-template results of every run, in order."""
+        for a in atom_batches:
+            self.plan.run_host_async(a)
+        return self.plan.wait()
+
     def run_device(self, d_atoms, d_results, use_graph=True):
         """Device buffers (torch tensors or raw pointers); asynchronous on the
         handle's stream.  ``d_results`` holds n_templates records of 40 bytes."""

@@ -27,6 +27,11 @@ struct tcw_handle {
   cudaStream_t stream = nullptr;
   cudaStream_t side_stream = nullptr;  // second branch of batched runs
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+  // pipelined host-buffer runs: uploads on their own stream, ordered after
+  // the previous run's prefix/repack kernels (the readers of the atoms)
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t consumed_ev = nullptr, copied_ev = nullptr;
+  bool consumed_pending = false;
   int prio_high = 0, prio_low = 0;
   char *d_ws = nullptr;
   size_t ws_cap = 0;
@@ -384,7 +389,10 @@ int tcw_create(tcw_handle **out, int device) {
       cudaStreamCreateWithPriority(&h->side_stream, cudaStreamNonBlocking, h->prio_low) !=
           cudaSuccess ||
       cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&h->join_ev, cudaEventDisableTiming) != cudaSuccess) {
+      cudaEventCreateWithFlags(&h->join_ev, cudaEventDisableTiming) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->consumed_ev, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->copied_ev, cudaEventDisableTiming) != cudaSuccess) {
     cudaGetLastError();
     tcw_destroy(h);
     return TCW_ERR_CUDA;
@@ -406,6 +414,12 @@ int tcw_destroy(tcw_handle *h) {
   }
   if (h->fork_ev) cudaEventDestroy(h->fork_ev);
   if (h->join_ev) cudaEventDestroy(h->join_ev);
+  if (h->copy_stream) {
+    cudaStreamSynchronize(h->copy_stream);
+    cudaStreamDestroy(h->copy_stream);
+  }
+  if (h->consumed_ev) cudaEventDestroy(h->consumed_ev);
+  if (h->copied_ev) cudaEventDestroy(h->copied_ev);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   cudaGetLastError();
   delete h;
@@ -440,6 +454,26 @@ int tcw_sync(tcw_handle *h, int timeout_ms) {
       return set_err(h, TCW_ERR_TIMEOUT, "stream not done after %d ms", timeout_ms);
     std::this_thread::sleep_for(std::chrono::microseconds(50));
   }
+}
+
+int tcw_pinned_alloc(void **ptr, size_t bytes) {
+  if (!ptr) return TCW_ERR_INVALID_ARG;
+  *ptr = nullptr;
+  if (cudaHostAlloc(ptr, std::max<size_t>(bytes, 16), cudaHostAllocDefault) != cudaSuccess) {
+    cudaGetLastError();
+    *ptr = nullptr;
+    return TCW_ERR_ALLOC;
+  }
+  return TCW_OK;
+}
+
+int tcw_pinned_free(void *ptr) {
+  if (!ptr) return TCW_OK;
+  if (cudaFreeHost(ptr) != cudaSuccess) {
+    cudaGetLastError();
+    return TCW_ERR_CUDA;
+  }
+  return TCW_OK;
 }
 
 int tcw_debug_fail_alloc(tcw_handle *h, int n) {
@@ -886,12 +920,15 @@ static MapLaunch plan_launch(const tcw_handle *h, const tcw_plan *p, int window,
 // prefix -> repack -> (exp tiles on the main stream at high priority || rect
 // tiles on the side stream) -> finalize.  The exp tiles are the long ones;
 // the rect kernel's blocks fill SMs as exp blocks retire.
+// `inputs_read`, if set, is recorded once the atoms have been read (after
+// the prefix and repack kernels; the map kernels read only their outputs).
 static int plan_enqueue(tcw_handle *h, tcw_plan *p, const float *d_atoms, tcw_result *d_results,
-                        float *d_maps) {
+                        float *d_maps, cudaEvent_t inputs_read = nullptr) {
   TCW_CUDA(h, cudaMemsetAsync(p->d_counter, 0, 2 * sizeof(uint32_t), h->stream));
   TCW_CUDA(h, launch_prefix(p->d_T, p->d_rect_list, p->n_rect, d_atoms, p->d_P, p->prec,
                             h->stream));
   TCW_CUDA(h, launch_repack(p->d_T, p->d_exp_list, p->n_exp, d_atoms, p->d_A8, h->stream));
+  if (inputs_read) TCW_CUDA(h, cudaEventRecord(inputs_read, h->stream));
   // Both map kernels become ready together: the high-priority exp blocks
   // fill the GPU first, and the persistent rect blocks take the SMs that exp
   // blocks leave as the exp tile queue runs dry (its tail).
@@ -1207,6 +1244,50 @@ int tcw_plan_run_host(tcw_handle *h, tcw_plan *p, const float *atoms, tcw_result
   TCW_CUDA(h, cudaMemcpyAsync(results, p->d_res_out, sizeof(tcw_result) * p->n_templates,
                               cudaMemcpyDeviceToHost, h->stream));
   TCW_CUDA(h, cudaStreamSynchronize(h->stream));
+  return TCW_OK;
+}
+
+int tcw_plan_run_host_async(tcw_handle *h, tcw_plan *p, const float *atoms,
+                            tcw_result *results) {
+  if (!h || !p) return TCW_ERR_INVALID_ARG;
+  if (!atoms || !results) return set_err(h, TCW_ERR_INVALID_ARG, "null host pointer");
+  if (p->flags & TCW_FLAG_POSTERIORS)
+    return set_err(h, TCW_ERR_INVALID_ARG,
+                   "posteriors need the maps: run the plan with tcw_plan_run_maps");
+  if (p->device != h->device)
+    return set_err(h, TCW_ERR_INVALID_ARG, "plan and handle are on different devices");
+  int rc = set_device(h);
+  if (rc) return rc;
+  const size_t abytes = sizeof(float) * 7u * (size_t)p->n_atom_rows;
+  if (!p->d_atoms_in) {
+    void *a = nullptr, *r = nullptr;
+    rc = ws_alloc(h, &a, std::max<size_t>(abytes, 16));
+    if (rc) return rc;
+    rc = ws_alloc(h, &r, sizeof(tcw_result) * p->n_templates);
+    if (rc) {
+      cudaFree(a);
+      return rc;
+    }
+    p->d_atoms_in = static_cast<float *>(a);
+    p->d_res_out = static_cast<tcw_result *>(r);
+  }
+  // the upload may start as soon as the previous run has read its atoms, so
+  // it overlaps that run's map kernels
+  if (h->consumed_pending) TCW_CUDA(h, cudaStreamWaitEvent(h->copy_stream, h->consumed_ev, 0));
+  TCW_CUDA(h, cudaMemcpyAsync(p->d_atoms_in, atoms, abytes, cudaMemcpyHostToDevice,
+                              h->copy_stream));
+  TCW_CUDA(h, cudaEventRecord(h->copied_ev, h->copy_stream));
+  TCW_CUDA(h, cudaStreamWaitEvent(h->stream, h->copied_ev, 0));
+  // the compensated map kernels read only the prefix and repacked rows; the
+  // uncompensated exp kernel reads the atoms themselves
+  const bool maps_read_atoms = p->prec == kPrecPlain32;
+  rc = plan_enqueue(h, p, p->d_atoms_in, p->d_res_out, nullptr,
+                    maps_read_atoms ? nullptr : h->consumed_ev);
+  if (rc) return rc;
+  if (maps_read_atoms) TCW_CUDA(h, cudaEventRecord(h->consumed_ev, h->stream));
+  h->consumed_pending = true;
+  TCW_CUDA(h, cudaMemcpyAsync(results, p->d_res_out, sizeof(tcw_result) * p->n_templates,
+                              cudaMemcpyDeviceToHost, h->stream));
   return TCW_OK;
 }
 

@@ -290,3 +290,32 @@ def test_one_shot_map_batched_equals_the_plan(batch):
     assert np.array_equal(max2F, 2.0 * res["maxF"])
     assert np.array_equal(argmax, res["argmax"])
     assert np.array_equal(lnB, res["lnBtSG"])
+
+
+def test_pipelined_runs_equal_synchronous_runs(batch):
+    """tcw_plan_run_host_async: each upload overlaps the previous run's map
+    kernels; every run's results equal a synchronous run on the same atoms."""
+    rng = np.random.default_rng(5)
+    arrays = []
+    for _ in range(4):
+        a = batch.atoms.copy()
+        a[:, 3:] *= rng.uniform(0.5, 2.0, size=(a.shape[0], 4)).astype(np.float32)
+        arrays.append(a)
+    out = batch.run_pipelined(arrays)
+    for a, r in zip(arrays, out):
+        ref = batch.run(a)
+        for key in ("maxF", "argmax", "lnBtSG"):
+            assert np.array_equal(r[key], ref[key]), key
+    assert not np.array_equal(out[0]["maxF"], out[1]["maxF"])
+    # a synchronous run between pipelined ones, page-locked atoms
+    from pyfstat_gb300 import _lib
+
+    pinned = _lib.pinned_empty(arrays[2].shape)
+    pinned[:] = arrays[2]
+    batch.plan.run_host_async(pinned)
+    mid = batch.run(arrays[3])
+    batch.plan.run_host_async(arrays[0])
+    r0, r1 = batch.plan.wait()
+    assert np.array_equal(r0["maxF"], out[2]["maxF"])
+    assert np.array_equal(mid["maxF"], out[3]["maxF"])
+    assert np.array_equal(r1["maxF"], out[0]["maxF"])
