@@ -950,8 +950,8 @@ TCW_HD void exp_column2(const float *__restrict__ atoms8, const Geom &g,
       if (e != Lp || !pinit) {
         if (pinit && e == Lp + 1u)
           pw = ff_mul(pw, k.r1);
-        else if (pinit && e + 1u == Lp && k.has_inv)
-          pw = ff_mul(pw, k.r1inv);
+        else if (pinit && e + 1u == Lp && (uint64_t)g.TAtom < 60ull * tau)
+          pw = ff_mul(pw, ff_recip(k.r1));  // r^-1 rebuilt here: no register held for it
         else
           pw = ff_pow(k.r1, e);
         Lp = e;
