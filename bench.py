@@ -52,6 +52,10 @@ def parse():
                    help="templates timed with the plain per-template kernel")
     p.add_argument("--window", choices=["both", "rect", "exp"], default="both",
                    help="restrict the workload to one window type (breakdown runs)")
+    p.add_argument("--case", choices=["plain-rect", "plain-exp"], default=None,
+                   help="instead of the benchmark: time one single-template map with the map "
+                        "written (8192 t0 x 4096 tau over one year of two-detector data; the "
+                        "134 MB map exceeds L2), for the memory-side profile of the plain kernel")
     p.add_argument("--tile", type=str, default="auto",
                    help="tile config as JSON, 'auto' for the autotuner (default), "
                         "'default' for the library defaults")
@@ -564,9 +568,66 @@ def run_ours(args, ws, rank, local):
         torch.distributed.destroy_process_group()
 
 
+def run_case(args):
+    """One plain single-template map (map written), CUDA-event timed: the
+    write bandwidth it reaches against the measured HBM copy peak."""
+    import torch
+
+    from pyfstat_gb300 import _lib, synth
+    from pyfstat_gb300.batched import template_grids
+
+    t = dict(synth.precision_templates(1)[0], window=1 if args.case == "plain-rect" else 2)
+    t0s, taus = template_grids(t)
+    N_t0, N_tau = len(t0s), len(taus)
+    dev = torch.device("cuda", 0)
+    h = _lib.Handle(0)
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    h.set_stream(stream.cuda_stream)
+    A = torch.from_numpy(np.ascontiguousarray(t["atoms"], np.float32)).to(dev)
+    d_t0 = torch.from_numpy(t0s.view(np.int32)).to(dev)
+    d_tau = torch.from_numpy(taus.view(np.int32)).to(dev)
+    F = torch.empty((N_t0, N_tau), dtype=torch.float32, device=dev)
+    res = torch.zeros(5, dtype=torch.float64, device=dev)
+
+    def call():
+        h.map_plain(A, A.shape[0], t["TAtom"], t["t0_data"], t["window"], d_t0, N_t0, d_tau,
+                    N_tau, F, res, flags=_lib.TCW_FLAG_LNBTSG)
+
+    for _ in range(max(3, args.warmup)):
+        call()
+    torch.cuda.synchronize(dev)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        call()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1) / args.steps
+    map_bytes = 4.0 * N_t0 * N_tau
+    hbm = None
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            hbm = json.load(f).get("hbm_gbs")
+    except (OSError, ValueError):
+        pass
+    gbs = map_bytes / (ms * 1e-3) / 1e9
+    print(json.dumps({"case": args.case, "N_t0": N_t0, "N_tau": N_tau,
+                      "numAtoms": int(A.shape[0]), "ms_per_call": ms,
+                      "cells_per_s": N_t0 * N_tau / (ms * 1e-3), "map_bytes": map_bytes,
+                      "map_write_gbs": gbs, "hbm_peak_gbs": hbm,
+                      "frac_of_hbm": (gbs / hbm) if hbm else None}), flush=True)
+    h.close()
+
+
 def main():
     args = parse()
     ws, rank, local = dist_env()
+    if args.case:
+        if rank == 0:
+            run_case(args)
+        return
     if args.impl == "reference":
         run_reference(args, ws, rank)
     else:
