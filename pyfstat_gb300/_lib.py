@@ -431,9 +431,9 @@ class Plan:
         if k == len(self._slots):
             self._slots.append(pinned_empty(self.n_templates, RESULT_DTYPE))
         slot = self._slots[k]
-        self._inflight.append(atoms7)
         check(load().tcw_plan_run_host_async(self.handle.ptr, self._p, atoms7.ctypes.data,
                                              slot.ctypes.data), self.handle.ptr)
+        self._inflight.append(atoms7)
 
     def wait(self, timeout_ms=600000):
         """Waits for the pipelined runs; their results (copies), in order."""

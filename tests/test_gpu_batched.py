@@ -319,3 +319,20 @@ def test_pipelined_runs_equal_synchronous_runs(batch):
     assert np.array_equal(r0["maxF"], out[2]["maxF"])
     assert np.array_equal(mid["maxF"], out[3]["maxF"])
     assert np.array_equal(r1["maxF"], out[0]["maxF"])
+
+
+def test_pipelined_run_rejects_posterior_plans_and_handle_survives(batch):
+    from pyfstat_gb300 import _lib
+
+    b2 = TransientMapBatch(small_templates(), handle=batch.handle,
+                           flags=_lib.TCW_FLAG_LNBTSG | _lib.TCW_FLAG_POSTERIORS)
+    try:
+        with pytest.raises(_lib.TcwError) as e:
+            b2.plan.run_host_async(b2.atoms)
+        assert e.value.code == _lib.TCW_ERR_INVALID_ARG
+        assert b2.plan.wait() == []
+    finally:
+        b2.close()
+    out = batch.run_pipelined([batch.atoms])
+    ref = batch.run()
+    assert np.array_equal(out[0]["maxF"], ref["maxF"])
