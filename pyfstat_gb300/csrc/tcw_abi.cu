@@ -30,7 +30,7 @@ struct tcw_handle {
   // pipelined host-buffer runs: uploads on their own stream, ordered after
   // the previous run's prefix/repack kernels (the readers of the atoms)
   cudaStream_t copy_stream = nullptr;
-  cudaEvent_t consumed_ev = nullptr, copied_ev = nullptr;
+  cudaEvent_t consumed_ev = nullptr, consumed_side_ev = nullptr, copied_ev = nullptr;
   bool consumed_pending = false;
   int prio_high = 0, prio_low = 0;
   char *d_ws = nullptr;
@@ -392,6 +392,7 @@ int tcw_create(tcw_handle **out, int device) {
       cudaEventCreateWithFlags(&h->join_ev, cudaEventDisableTiming) != cudaSuccess ||
       cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&h->consumed_ev, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->consumed_side_ev, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&h->copied_ev, cudaEventDisableTiming) != cudaSuccess) {
     cudaGetLastError();
     tcw_destroy(h);
@@ -419,6 +420,7 @@ int tcw_destroy(tcw_handle *h) {
     cudaStreamDestroy(h->copy_stream);
   }
   if (h->consumed_ev) cudaEventDestroy(h->consumed_ev);
+  if (h->consumed_side_ev) cudaEventDestroy(h->consumed_side_ev);
   if (h->copied_ev) cudaEventDestroy(h->copied_ev);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   cudaGetLastError();
@@ -917,23 +919,28 @@ static MapLaunch plan_launch(const tcw_handle *h, const tcw_plan *p, int window,
   return ml;
 }
 
-// prefix -> repack -> (exp tiles on the main stream at high priority || rect
-// tiles on the side stream) -> finalize.  The exp tiles are the long ones;
-// the rect kernel's blocks fill SMs as exp blocks retire.
-// `inputs_read`, if set, is recorded once the atoms have been read (after
-// the prefix and repack kernels; the map kernels read only their outputs).
+// (repack -> exp tiles on the main stream at high priority) || (prefix ->
+// rect tiles on the side stream) -> finalize.  The exp tiles are the long
+// ones; the rect kernel's blocks fill SMs as exp blocks retire.
+// `inputs_read` / `inputs_read_side`, if set, are recorded once the atoms
+// have been read (after the repack kernel on the main stream and the prefix
+// kernel on the side stream; the map kernels read only their outputs).
 static int plan_enqueue(tcw_handle *h, tcw_plan *p, const float *d_atoms, tcw_result *d_results,
-                        float *d_maps, cudaEvent_t inputs_read = nullptr) {
+                        float *d_maps, cudaEvent_t inputs_read = nullptr,
+                        cudaEvent_t inputs_read_side = nullptr) {
   TCW_CUDA(h, cudaMemsetAsync(p->d_counter, 0, 2 * sizeof(uint32_t), h->stream));
-  TCW_CUDA(h, launch_prefix(p->d_T, p->d_rect_list, p->n_rect, d_atoms, p->d_P, p->prec,
-                            h->stream));
-  TCW_CUDA(h, launch_repack(p->d_T, p->d_exp_list, p->n_exp, d_atoms, p->d_A8, h->stream));
-  if (inputs_read) TCW_CUDA(h, cudaEventRecord(inputs_read, h->stream));
-  // Both map kernels become ready together: the high-priority exp blocks
-  // fill the GPU first, and the persistent rect blocks take the SMs that exp
-  // blocks leave as the exp tile queue runs dry (its tail).
+  // Two branches from the start: repack -> exp tiles (main stream, high
+  // priority) || prefix -> rect tiles (side stream, low priority), so the
+  // exp kernel does not wait for the rect templates' prefix scans; the
+  // persistent rect blocks take the SMs that exp blocks leave as the exp
+  // tile queue runs dry (its tail).
   TCW_CUDA(h, cudaEventRecord(h->fork_ev, h->stream));
   TCW_CUDA(h, cudaStreamWaitEvent(h->side_stream, h->fork_ev, 0));
+  TCW_CUDA(h, launch_repack(p->d_T, p->d_exp_list, p->n_exp, d_atoms, p->d_A8, h->stream));
+  if (inputs_read) TCW_CUDA(h, cudaEventRecord(inputs_read, h->stream));
+  TCW_CUDA(h, launch_prefix(p->d_T, p->d_rect_list, p->n_rect, d_atoms, p->d_P, p->prec,
+                            h->side_stream));
+  if (inputs_read_side) TCW_CUDA(h, cudaEventRecord(inputs_read_side, h->side_stream));
   TCW_CUDA(h, launch_map(TCW_WINDOW_EXP, plan_launch(h, p, TCW_WINDOW_EXP, d_atoms, d_maps),
                          h->stream));
   TCW_CUDA(h, launch_map(TCW_WINDOW_RECT, plan_launch(h, p, TCW_WINDOW_RECT, d_atoms, d_maps),
@@ -1273,7 +1280,10 @@ int tcw_plan_run_host_async(tcw_handle *h, tcw_plan *p, const float *atoms,
   }
   // the upload may start as soon as the previous run has read its atoms, so
   // it overlaps that run's map kernels
-  if (h->consumed_pending) TCW_CUDA(h, cudaStreamWaitEvent(h->copy_stream, h->consumed_ev, 0));
+  if (h->consumed_pending) {
+    TCW_CUDA(h, cudaStreamWaitEvent(h->copy_stream, h->consumed_ev, 0));
+    TCW_CUDA(h, cudaStreamWaitEvent(h->copy_stream, h->consumed_side_ev, 0));
+  }
   TCW_CUDA(h, cudaMemcpyAsync(p->d_atoms_in, atoms, abytes, cudaMemcpyHostToDevice,
                               h->copy_stream));
   TCW_CUDA(h, cudaEventRecord(h->copied_ev, h->copy_stream));
@@ -1282,9 +1292,13 @@ int tcw_plan_run_host_async(tcw_handle *h, tcw_plan *p, const float *atoms,
   // uncompensated exp kernel reads the atoms themselves
   const bool maps_read_atoms = p->prec == kPrecPlain32;
   rc = plan_enqueue(h, p, p->d_atoms_in, p->d_res_out, nullptr,
-                    maps_read_atoms ? nullptr : h->consumed_ev);
+                    maps_read_atoms ? nullptr : h->consumed_ev,
+                    maps_read_atoms ? nullptr : h->consumed_side_ev);
   if (rc) return rc;
-  if (maps_read_atoms) TCW_CUDA(h, cudaEventRecord(h->consumed_ev, h->stream));
+  if (maps_read_atoms) {
+    TCW_CUDA(h, cudaEventRecord(h->consumed_ev, h->stream));
+    TCW_CUDA(h, cudaEventRecord(h->consumed_side_ev, h->stream));
+  }
   h->consumed_pending = true;
   TCW_CUDA(h, cudaMemcpyAsync(results, p->d_res_out, sizeof(tcw_result) * p->n_templates,
                               cudaMemcpyDeviceToHost, h->stream));
