@@ -69,3 +69,9 @@ def test_client_map_matches_fp64_oracle(client, tmp_path, oracle, window):
     assert argmax_ok(r["argmax"], F64)
     assert r["lnBtSG"] == pytest.approx(oracle.lnBtSG(F64), rel=REL_TOL)
     assert abs(r["F00"] - F64[0, 0]) <= REL_TOL * abs(F64[0, 0])
+    # the batched plan from C: template `window - 1` is this window's map
+    assert r["plan"] == 0, r
+    assert r["pipelined_equal"] is True
+    k = window - 1
+    assert abs(r["plan_maxF"][k] - F64.max()) <= REL_TOL * F64.max()
+    assert argmax_ok(r["plan_argmax"][k], F64)
