@@ -93,6 +93,7 @@ __global__ void __launch_bounds__(256) prefix_kernel(const TemplateDev *__restri
     loc[c] = ff_zero();
     sabs[c] = 0.0f;
   }
+#pragma unroll 4
   for (uint32_t i = i0; i < i1; i++) {
 #pragma unroll
     for (int c = 0; c < 7; c++) {
@@ -154,6 +155,7 @@ __global__ void __launch_bounds__(256) prefix_kernel(const TemplateDev *__restri
     for (int k = 0; k < 4; k++) o[k] = make_float4(r[4 * k], r[4 * k + 1], r[4 * k + 2], r[4 * k + 3]);
   };
 
+#pragma unroll 4
   for (uint32_t i = i0; i < i1; i++) {
     write_row(i);
 #pragma unroll
@@ -803,11 +805,79 @@ int map_blocks_per_sm(int window, int prec) {
                                    : blocks_per_sm_win<TCW_WINDOW_EXP>(prec);
 }
 
+// One template, one block: the partials of a large single-template call (up
+// to thousands of tiles) merged by 256 threads; warps' results combined in
+// warp order.
+__global__ void __launch_bounds__(256) finalize_one_kernel(const TemplateDev *__restrict__ T,
+                                                           const Partial *__restrict__ parts,
+                                                           tcw_result *__restrict__ results) {
+  __shared__ float s_best[8];
+  __shared__ int64_t s_bidx[8];
+  __shared__ double s_sum[8];
+  const TemplateDev t = T[0];
+  const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+  float best = -INFINITY;
+  int64_t bidx = INT64_MAX;
+  for (uint32_t k = threadIdx.x; k < t.n_parts; k += blockDim.x) {
+    const Partial p = parts[t.part_off + k];
+    if (p.maxF > best || (p.maxF == best && p.argmax < bidx)) {
+      best = p.maxF;
+      bidx = p.argmax;
+    }
+  }
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) {
+    float ob = __shfl_xor_sync(0xffffffffu, best, d);
+    int64_t oi = __shfl_xor_sync(0xffffffffu, bidx, d);
+    if (ob > best || (ob == best && oi < bidx)) {
+      best = ob;
+      bidx = oi;
+    }
+  }
+  if (lane == 0) {
+    s_best[wid] = best;
+    s_bidx[wid] = bidx;
+  }
+  __syncthreads();
+  best = s_best[0];
+  bidx = s_bidx[0];
+  for (uint32_t w = 1; w < blockDim.x / 32u; w++)
+    if (s_best[w] > best || (s_best[w] == best && s_bidx[w] < bidx)) {
+      best = s_best[w];
+      bidx = s_bidx[w];
+    }
+  double S = 0.0;
+  for (uint32_t k = threadIdx.x; k < t.n_parts; k += blockDim.x) {
+    const Partial p = parts[t.part_off + k];
+    if (p.s > 0.0) S += p.s * (double)exp2f((p.maxF - best) * kLog2e);
+  }
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) S += __shfl_xor_sync(0xffffffffu, S, d);
+  if (lane == 0) s_sum[wid] = S;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    S = 0.0;
+    for (uint32_t w = 0; w < blockDim.x / 32u; w++) S += s_sum[w];
+    tcw_result r;
+    r.maxF = best;
+    r.argmax = bidx;
+    r.lnBtSG = log(70.0 / ((double)t.N_t0 * (double)t.N_tau)) + (double)best + log(S);
+    r.t0_mp_idx = -1;
+    r.tau_mp_idx = -1;
+    r.status = 0;
+    results[0] = r;
+  }
+}
+
 cudaError_t launch_finalize(const TemplateDev *d_T, uint32_t n_templates, const Partial *d_parts,
                             void *d_results, cudaStream_t stream) {
   if (n_templates == 0) return cudaSuccess;
-  finalize_kernel<<<(n_templates + 3u) / 4u, 128, 0, stream>>>(
-      d_T, n_templates, d_parts, reinterpret_cast<tcw_result *>(d_results));
+  if (n_templates == 1)
+    finalize_one_kernel<<<1, 256, 0, stream>>>(d_T, d_parts,
+                                               reinterpret_cast<tcw_result *>(d_results));
+  else
+    finalize_kernel<<<(n_templates + 3u) / 4u, 128, 0, stream>>>(
+        d_T, n_templates, d_parts, reinterpret_cast<tcw_result *>(d_results));
   return cudaGetLastError();
 }
 
