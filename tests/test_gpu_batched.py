@@ -336,3 +336,52 @@ def test_pipelined_run_rejects_posterior_plans_and_handle_survives(batch):
     out = batch.run_pipelined([batch.atoms])
     ref = batch.run()
     assert np.array_equal(out[0]["maxF"], ref["maxF"])
+
+
+def random_templates(seed):
+    """Random geometries in the style of the host tests' random grids: t0
+    grids off the atom grid and starting before the data (u32 wrap of
+    t0 - t0_data), taus with dtau = 0 included, gap runs of zero atoms."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(24):
+        t0_data, A = synth.merged_atoms(1000 * seed + k, int(rng.integers(20, 300)),
+                                        int(rng.integers(1, 3)),
+                                        gap_frac=float(rng.uniform(0, 0.5)))
+        A = A.copy()
+        for _ in range(int(rng.integers(0, 4))):
+            s = int(rng.integers(0, A.shape[0]))
+            A[s:s + int(rng.integers(1, 40))] = 0
+        nt0, ntau = int(rng.integers(1, 60)), int(rng.integers(1, 60))
+        t0 = int(t0_data + rng.integers(-5000, 3000))
+        t0s = (t0 + np.arange(nt0) * int(rng.integers(1, 4000))).astype(np.uint32)
+        taus = (int(rng.integers(1, 5000)) + np.arange(ntau) * int(rng.integers(0, 8000))
+                ).astype(np.uint32)
+        out.append(dict(window=1 + k % 2, atoms=A, TAtom=1800, t0_data=t0_data, t0s=t0s,
+                        taus=taus))
+    return out
+
+
+@pytest.mark.parametrize("seed,cfg", [
+    (1, None),
+    (2, dict(rect_tn=5, rect_tm=32, exp_tn=32, exp_rows=7, blocks_per_sm=3)),
+    (3, dict(rect_tn=64, rect_tm=128, exp_tn=64, exp_rows=0, blocks_per_sm=8)),
+])
+def test_random_geometries_in_one_launch(oracle, seed, cfg):
+    """Random geometries (u32 wrap, off-grid steps, dtau = 0, gaps) of both
+    windows in one persistent launch, against the FP64 oracle."""
+    templates = random_templates(seed)
+    b = TransientMapBatch(templates, tile_config=cfg)
+    try:
+        res = b.run()
+    finally:
+        b.close()
+    for k, t in enumerate(templates):
+        F64, cond = oracle.map_f64(t["atoms"], 1800, t["t0_data"], t["window"], t["t0s"],
+                                   t["taus"], with_cond=True)
+        band = np.abs(cond / 1e4 - 1) < 1e-5
+        assert float(res["maxF"][k]) == pytest.approx(F64.max(), rel=REL_TOL), (seed, k)
+        if not band.any():
+            assert argmax_ok(res["argmax"][k], F64), (seed, k)
+            assert float(res["lnBtSG"][k]) == pytest.approx(oracle.lnBtSG(F64), rel=REL_TOL,
+                                                            abs=1e-6), (seed, k)
