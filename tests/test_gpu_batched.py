@@ -292,9 +292,17 @@ def test_one_shot_map_batched_equals_the_plan(batch):
     assert np.array_equal(lnB, res["lnBtSG"])
 
 
-def test_pipelined_runs_equal_synchronous_runs(batch):
+@pytest.mark.parametrize("uncompensated", [False, True])
+def test_pipelined_runs_equal_synchronous_runs(batch, uncompensated):
     """tcw_plan_run_host_async: each upload overlaps the previous run's map
-    kernels; every run's results equal a synchronous run on the same atoms."""
+    kernels (waits for them too where they read the atoms themselves: the
+    uncompensated variant); every run's results equal a synchronous run on
+    the same atoms."""
+    from pyfstat_gb300 import _lib
+
+    if uncompensated:
+        batch = TransientMapBatch(small_templates(), handle=batch.handle,
+                                  flags=_lib.TCW_FLAG_LNBTSG | _lib.TCW_FLAG_UNCOMPENSATED)
     rng = np.random.default_rng(5)
     arrays = []
     for _ in range(4):
@@ -319,6 +327,8 @@ def test_pipelined_runs_equal_synchronous_runs(batch):
     assert np.array_equal(r0["maxF"], out[2]["maxF"])
     assert np.array_equal(mid["maxF"], out[3]["maxF"])
     assert np.array_equal(r1["maxF"], out[0]["maxF"])
+    if uncompensated:
+        batch.close()
 
 
 def test_pipelined_run_rejects_posterior_plans_and_handle_survives(batch):
