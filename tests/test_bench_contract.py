@@ -64,3 +64,18 @@ def test_gpu_arm_line():
     assert d["gpu_launches"] >= 2 * 5
     c = d["clocks"]
     assert "sm_mhz" in c and "sm_max_mhz" in c and isinstance(c["reasons"], list)
+
+
+@pytest.mark.gpu
+def test_gpu_single_template_case_line():
+    lines = []
+    for case in ("plain-rect", "plain-exp"):
+        r = subprocess.run([sys.executable, os.path.join(REPO, "bench.py"), "--case", case,
+                            "--steps", "2", "--warmup", "3"], cwd=REPO, capture_output=True,
+                           text=True, timeout=600)
+        assert r.returncode == 0, r.stderr[-2000:]
+        d = json.loads([l for l in r.stdout.splitlines() if l.startswith("{")][-1])
+        assert d["case"] == case and d["N_t0"] == 8192 and d["N_tau"] == 4096
+        assert d["ms_per_call"] > 0 and d["map_bytes"] == 4.0 * 8192 * 4096
+        assert d["map_write_gbs"] == pytest.approx(d["map_bytes"] / d["ms_per_call"] / 1e6)
+        lines.append(d)
