@@ -68,7 +68,6 @@ def test_gpu_arm_line():
 
 @pytest.mark.gpu
 def test_gpu_single_template_case_line():
-    lines = []
     for case in ("plain-rect", "plain-exp"):
         r = subprocess.run([sys.executable, os.path.join(REPO, "bench.py"), "--case", case,
                             "--steps", "2", "--warmup", "3"], cwd=REPO, capture_output=True,
@@ -78,4 +77,3 @@ def test_gpu_single_template_case_line():
         assert d["case"] == case and d["N_t0"] == 8192 and d["N_tau"] == 4096
         assert d["ms_per_call"] > 0 and d["map_bytes"] == 4.0 * 8192 * 4096
         assert d["map_write_gbs"] == pytest.approx(d["map_bytes"] / d["ms_per_call"] / 1e6)
-        lines.append(d)
