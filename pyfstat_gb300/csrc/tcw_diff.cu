@@ -125,8 +125,20 @@ constexpr int kDiffBlock = 128;
 // injected term to FP64 accuracy.
 constexpr uint32_t kDiffSlots = TCW_DIFF_SLOTS;
 
+// Minimum resident blocks per SM asked of the register allocator, per pass
+// (build-time tunables; 1 leaves the allocation to ptxas).
+#ifndef TCW_DIFF_MIN_BLOCKS_FWD
+#define TCW_DIFF_MIN_BLOCKS_FWD 5
+#endif
+#ifndef TCW_DIFF_MIN_BLOCKS_BWD
+#define TCW_DIFF_MIN_BLOCKS_BWD 1
+#endif
+constexpr int diff_min_blocks(int pass) {
+  return pass == 0 ? TCW_DIFF_MIN_BLOCKS_FWD : TCW_DIFF_MIN_BLOCKS_BWD;
+}
+
 template <int kPass>
-__global__ void __launch_bounds__(kDiffBlock)
+__global__ void __launch_bounds__(kDiffBlock, diff_min_blocks(kPass))
     diff_kernel(const DiffTemplate *__restrict__ T, const DiffItem *__restrict__ items,
                 uint32_t n_items, uint32_t *__restrict__ counter, const float *__restrict__ atoms,
                 const uint32_t *__restrict__ t0s_all, double temp, DiffPartial *__restrict__ parts,
@@ -412,7 +424,7 @@ __device__ __forceinline__ void flush_diff(double *D, uint32_t row, const double
 }
 
 template <int kPass>
-__global__ void __launch_bounds__(kDiffBlock)
+__global__ void __launch_bounds__(kDiffBlock, diff_min_blocks(kPass))
     rect_diff_kernel(const DiffTemplate *__restrict__ T, const DiffItem *__restrict__ items,
                      uint32_t n_items, uint32_t *__restrict__ counter,
                      const float *__restrict__ atoms, const uint32_t *__restrict__ t0s_all,
