@@ -926,7 +926,6 @@ TCW_HD void exp_column2(const float *__restrict__ atoms8, const Geom &g,
   FF pw{1.0f, 0.0f}, p2{1.0f, 0.0f};
   F2 ph[2], nph[2], pl[2];           // p2 and pw, packed
   bool pinit = false;
-  bool init = false;
   for (uint32_t mm = m_end; mm > m_begin; mm--) {
     const uint32_t m = mm - 1u;
     const uint32_t t0 = t0s[m];
@@ -937,12 +936,12 @@ TCW_HD void exp_column2(const float *__restrict__ atoms8, const Geom &g,
       continue;
     }
     const uint32_t top = hi + 1u;
-    if (!init || top > wtop || lo > wlo || top <= wlo) {
+    // (the first row restarts too: top >= 1 > wtop = 0)
+    if (top > wtop || lo > wlo || top <= wlo) {
       wlo = wtop = top;
       nz = 0xFFFFFFFFu;
       W0 = W2 = W3 = FF2{z, z};
       Wc = FF{0.0f, 0.0f};
-      init = true;
     }
     while (wtop > top) {
       wtop--;
