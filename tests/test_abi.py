@@ -91,3 +91,23 @@ def test_release_build_has_no_device_checks():
     n = ctypes.c_uint32(7)
     assert _lib.load().tcw_debug_check_failures(ctypes.byref(n)) == _lib.TCW_ERR_UNSUPPORTED
     assert n.value == 0
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    """With the CUDA library absent the product path raises; there is no
+    other implementation to fall back to."""
+    import subprocess
+    import sys
+
+    code = ("from pyfstat_gb300 import _lib\n"
+            "try:\n"
+            "    _lib.load()\n"
+            "except RuntimeError as e:\n"
+            "    print('raised', e)\n"
+            "else:\n"
+            "    print('loaded')\n")
+    env = dict(os.environ, PYFSTAT_GB300_LIB=str(tmp_path / "absent.so"))
+    r = subprocess.run([sys.executable, "-c", code], cwd=REPO, env=env, capture_output=True,
+                       text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.startswith("raised") and "missing" in r.stdout
