@@ -109,7 +109,9 @@ int tcw_device_info(int device, char *name, size_t name_len, int *cc_major, int 
 /* Handle: owns a CUDA stream and a grow-only device workspace on `device`
  * (the pycuda context of tcw:419-470 and its per-call allocations,
  * tcw:861-912).  tcw_set_stream takes a caller's cudaStream_t, NULL for the
- * handle's own stream, or cudaStreamLegacy for the legacy default stream. */
+ * handle's own stream, or cudaStreamLegacy for the legacy default stream.
+ * tcw_create returns TCW_ERR_NO_DEVICE unless `device` has compute
+ * capability 10.3: the kernels are built for sm_103a only. */
 int tcw_create(tcw_handle **h, int device);
 int tcw_destroy(tcw_handle *h);
 int tcw_get_stream(tcw_handle *h, void **stream);
@@ -296,8 +298,12 @@ int tcw_probe_peaks(int device, double *fp32_tflops, double *fp64_tflops, double
  * rows (rect) or 32 B x numAtoms atom rows (exp), 56 B per tile, and with
  * TCW_FLAG_POSTERIORS 8 B x (N_t0 + ceil(N_t0/64) x N_tau) -- is rejected
  * with TCW_ERR_OVERFLOW.  The first call on a device looks the array's
- * address up: make it before any stream capture.  Calls share the array:
- * calls whose work overlaps on the GPU race and must be serialised. */
+ * address up and caches it per device: make it before any stream capture.
+ * The cached address is that of the device's primary context (the one the
+ * CUDA runtime uses); it is not valid after cudaDeviceReset of the device or
+ * under another context made current through the driver API.  Calls share
+ * the array: calls whose work overlaps on the GPU race and must be
+ * serialised. */
 int tcw_map_plain_noalloc(void *stream, const float *d_atoms, uint32_t numAtoms, uint32_t TAtom,
                           uint32_t t0_data, int window, const uint32_t *d_t0s, uint32_t N_t0,
                           const uint32_t *d_taus, uint32_t N_tau, float *d_Fmn,

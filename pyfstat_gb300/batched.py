@@ -6,8 +6,10 @@ call_compute_transient_fstat_map once each).  :class:`TransientMapBatch`
 takes all templates at once: the geometry (atom counts, windows, grids) is
 fixed in a plan; each run takes the concatenated atoms and returns, per
 template, maxF (2F = 2 maxF), the flat argmax and lnBtSG (FP64), without
-writing any map.  A run is one CUDA graph of a prefix kernel, the persistent
-map kernel and a finalize kernel.
+writing any map.  A run is one CUDA graph of five launches on two branches:
+(repack -> persistent exponential-window map kernel) and (prefix ->
+persistent rectangular-window map kernel), joined by a finalize kernel
+(plus the posterior kernels when maps are written).
 """
 
 import numpy as np

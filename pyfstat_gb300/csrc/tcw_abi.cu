@@ -371,7 +371,10 @@ int tcw_create(tcw_handle **out, int device) {
     return rc;
   }
   cudaDeviceProp prop;
-  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess || prop.major < 10) {
+  // The kernels are built for sm_103a only: architecture-specific code that
+  // loads on compute capability 10.3 and on no other device.
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess || prop.major != 10 ||
+      prop.minor != 3) {
     cudaGetLastError();
     delete h;
     return TCW_ERR_NO_DEVICE;

@@ -6,8 +6,10 @@
 //   map_kernel       the (t0, tau) cells of a list of tiles; a block owns one tile
 //                    (grid launch) or pulls tiles from an atomic counter
 //                    (persistent launch).  Rectangular tiles difference two prefix
-//                    rows per cell; exponential tiles run two backward double-word
-//                    recurrences per tau column.  Every block reduces its cells to
+//                    rows per cell; exponential tiles slide one double-word window
+//                    sum down each tau column (atoms enter at the lower window end
+//                    and leave at the upper end).  Every block (rect: every warp
+//                    of a persistent launch) reduces its cells to
 //                    (max F, first argmax, sum exp(F - max F)).
 //   repack_kernel    exponential templates' atoms into 32-byte rows (one 256-bit
 //                    load per recurrence step)

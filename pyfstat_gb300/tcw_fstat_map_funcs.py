@@ -136,14 +136,21 @@ def _optional_import(modulename):
         return False
 
 
+# The library is compiled for sm_103a only (architecture-specific code: it
+# loads on compute capability 10.3 and nowhere else).
+B200_COMPUTE_CAPABILITY = (10, 3)
+
+
 def _b200_available():
+    """True iff the library loads and a device it can run on is present
+    (the 'b200' row of _get_transient_fstat_map_features, tcw:351-358)."""
     try:
         n = _lib.device_count()
     except Exception as e:  # library missing or not loadable
         logger.debug(f"b200 library not available: {e}")
         return False
     for d in range(n):
-        if _lib.device_info(d)["cc"][0] >= 10:
+        if tuple(_lib.device_info(d)["cc"]) == B200_COMPUTE_CAPABILITY:
             return True
     return False
 
@@ -224,7 +231,7 @@ def init_transient_fstat_map_features(feature="lal", cudaDeviceName=None):
     if feature == "b200":
         if not features["b200"]:
             raise RuntimeError(
-                "b200 use was requested, but the CUDA library or a compute capability 10.x"
+                "b200 use was requested, but the CUDA library or a compute capability 10.3"
                 " device is not available.")
         devnum = _select_device(cudaDeviceName)
         if _current_context is not None:

@@ -1,10 +1,9 @@
 """Generate the golden fixtures in tests/golden/ from the reference itself.
 
-Run in a container that has the read-only PyFstat checkout (default
-/root/reference, override with PYFSTAT_REF) and the host build of its pycuda
-kernels (``make -C oracle ref``):
+Run where a PyFstat checkout is available, with PYFSTAT_REF naming it, after
+the host build of its pycuda kernels (``make -C oracle ref REF=$PYFSTAT_REF``):
 
-    python tests/golden/make_golden.py
+    PYFSTAT_REF=<checkout> python tests/golden/make_golden.py
 
 For every case it records
   * the F map of the reference's own kernels compiled for the host
@@ -33,7 +32,9 @@ import oracle as O  # noqa: E402
 from pyfstat_gb300 import synth  # noqa: E402
 from pyfstat_gb300.window import transientWindowRange_t, uniform_grid  # noqa: E402
 
-REF = os.environ.get("PYFSTAT_REF", "/root/reference")
+REF = os.environ.get("PYFSTAT_REF")
+if not REF:
+    sys.exit("set PYFSTAT_REF to the PyFstat checkout the fixtures are generated from")
 
 
 def load_reference_tcw():

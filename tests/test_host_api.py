@@ -135,3 +135,20 @@ def test_unknown_window_type_raises_before_any_gpu_work():
     wr = transientWindowRange_t(type=3)
     with pytest.raises(ValueError, match="Unknown window-type"):
         tcw.b200_compute_transient_fstat_map(multi, wr)
+
+
+@pytest.mark.parametrize("cc,expect", [((10, 3), True), ((10, 0), False), ((12, 0), False),
+                                       ((9, 0), False)])
+def test_b200_feature_requires_compute_capability_10_3(monkeypatch, cc, expect):
+    # the library holds sm_103a code only: a cc 10.0 (B200) or 12.x device
+    # cannot run it, so the 'b200' feature must be False there
+    from pyfstat_gb300 import _lib
+
+    monkeypatch.setattr(_lib, "device_count", lambda: 1)
+    monkeypatch.setattr(_lib, "device_info",
+                        lambda d: dict(name="fake", cc=cc, total_mem=1 << 30))
+    assert tcw._b200_available() is expect
+    assert tcw._get_transient_fstat_map_features()["b200"] is expect
+    if not expect:
+        with pytest.raises(RuntimeError, match="compute capability 10.3"):
+            tcw.init_transient_fstat_map_features("b200")
