@@ -144,29 +144,77 @@ def gpu_uuid(torch, dev):
 # ------------------------------------------------------------------ CPU baseline
 
 
-def cpu_baseline(templates, seconds, threads):
+def template_cost(t):
+    """CPU cost model of one template on the reference's path: rectangular
+    maps cost O(1) per cell (plus the running sums along tau); exponential
+    maps sum every atom of each cell's window (up to 3 tau / TAtom atoms)."""
+    from pyfstat_gb300.batched import template_grids
+
+    t0s, taus = template_grids(t)
+    cells = float(len(t0s)) * len(taus)
+    if t["window"] == 1:
+        return cells
+    win = np.minimum(3.0 * taus.astype(np.float64) / t["TAtom"], t["atoms"].shape[0])
+    return float(len(t0s)) * float(np.sum(np.maximum(win, 1.0)))
+
+
+def cpu_baseline(templates, seconds, threads, seed=2024):
     """The reference's per-template CPU path restated in C (oracle port: the
     pycuda kernels' FP32 arithmetic, OpenMP over rows/cells) plus its numpy
-    max/argmax/lnBtSG, over consecutive templates until ~`seconds`."""
+    max/argmax/lnBtSG, timed on a stratified random sample of the workload:
+    rectangular and exponential templates drawn alternately (seeded) until
+    ~`seconds` of CPU time.  The whole workload's time is estimated per window
+    type by a ratio estimator on the cost model (template_cost): sampled
+    seconds x (the window type's total cost / the sample's cost).  Returns
+    (cells/s of the whole workload, details)."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle as O
     from pyfstat_gb300.batched import template_grids
 
     O.build()
-    cells, used = 0, 0
-    t0 = time.perf_counter()
-    for t in templates:
-        t0s, taus = template_grids(t)
-        fn = O.rect_map_f32 if t["window"] == 1 else O.exp_map_f32
-        F = fn(t["atoms"], t["TAtom"], t["t0_data"], t0s, taus, nthreads=threads)
-        O.max_argmax(F)
-        O.lnBtSG(F)
-        cells += F.size
-        used += 1
-        if time.perf_counter() - t0 > seconds and used >= 2:
+    rng = np.random.default_rng(seed)
+    groups = {w: [k for k, t in enumerate(templates) if t["window"] == w] for w in (1, 2)}
+    order = {w: list(rng.permutation(ix)) for w, ix in groups.items() if ix}
+    cost = {w: {k: template_cost(templates[k]) for k in ix} for w, ix in groups.items()}
+    spent = {w: 0.0 for w in order}
+    scost = {w: 0.0 for w in order}
+    scells = {w: 0 for w in order}
+    used = {w: 0 for w in order}
+    t_start = time.perf_counter()
+    while any(order.values()):
+        for w in list(order):
+            if not order[w]:
+                continue
+            k = order[w].pop()
+            t = templates[k]
+            t0s, taus = template_grids(t)
+            fn = O.rect_map_f32 if w == 1 else O.exp_map_f32
+            a = time.perf_counter()
+            F = fn(t["atoms"], t["TAtom"], t["t0_data"], t0s, taus, nthreads=threads)
+            O.max_argmax(F)
+            O.lnBtSG(F)
+            spent[w] += time.perf_counter() - a
+            scost[w] += cost[w][k]
+            scells[w] += F.size
+            used[w] += 1
+        if time.perf_counter() - t_start > seconds and all(used[w] >= 2 for w in order):
             break
-    dt = time.perf_counter() - t0
-    return cells / dt, cells, used, dt
+    total_cells = sum(float(t["N_t0"]) * t["N_tau"] if "N_t0" in t else
+                      float(len(template_grids(t)[0])) * len(template_grids(t)[1])
+                      for t in templates)
+    est = {w: spent[w] * sum(cost[w].values()) / scost[w] for w in order}
+    value = total_cells / sum(est.values())
+    names = {1: "rect", 2: "exp"}
+    detail = {
+        "sample": (f"stratified seeded sample: {used.get(1, 0)} rect + {used.get(2, 0)} exp "
+                   f"templates ({sum(scells.values())} cells, {sum(spent.values()):.1f} s); "
+                   "whole-workload time per window type = sampled time x total cost / sampled "
+                   "cost (cost: cells for rect, cells x window length for exp)"),
+        "per_window_cells_per_s": {names[w]: scells[w] / spent[w] for w in order},
+        "estimated_workload_s": {names[w]: est[w] for w in order},
+        "templates_sampled": {names[w]: used[w] for w in order},
+    }
+    return value, detail
 
 
 def dropin_per_call(h, reps=20):
@@ -240,16 +288,45 @@ def cpu_model():
     return platform.processor() or platform.machine()
 
 
-def traffic_per_launch(kernel):
-    """DRAM bytes per launch of a map kernel from its committed ncu summary, if any."""
+# Sources whose compiled code the map-kernel profiles describe; each committed
+# summary records their hash ("kernel_source_sha16 = ...") at capture time.
+KERNEL_SOURCES = ("tcw_kernels.cu", "tcw_cell.h", "tcw_internal.h")
+
+
+def kernel_source_hash():
+    """First 16 hex digits of the SHA-256 of the map kernels' sources."""
+    import hashlib
+
+    h = hashlib.sha256()
+    for name in KERNEL_SOURCES:
+        with open(os.path.join(REPO, "pyfstat_gb300", "csrc", name), "rb") as f:
+            h.update(name.encode() + b"\0" + f.read())
+    return h.hexdigest()[:16]
+
+
+def profile_text(kernel):
     try:
         with open(TRAFFIC_FILES[kernel]) as f:
-            for line in f:
-                if line.strip().startswith("traffic_bytes_per_launch"):
-                    return float(line.split("=")[1].split()[0])
-    except (OSError, ValueError, IndexError, KeyError):
-        pass
-    return None
+            return f.read()
+    except (OSError, KeyError):
+        return ""
+
+
+def profile_is_current(kernel):
+    """True when the kernel's committed ncu summary was captured from the
+    sources built now (its recorded source hash equals the current one)."""
+    for line in profile_text(kernel).splitlines():
+        if line.strip().startswith("kernel_source_sha16"):
+            return line.split("=")[1].strip() == kernel_source_hash()
+    return False
+
+
+def traffic_per_launch(kernel):
+    """DRAM bytes per launch of a map kernel from its committed ncu summary,
+    or None when there is none or it was captured from other sources."""
+    if not profile_is_current(kernel):
+        return None
+    return profile_figure(kernel, "traffic_bytes_per_launch")
 
 
 def launches_per_step(n_rect, n_exp):
@@ -260,22 +337,26 @@ def launches_per_step(n_rect, n_exp):
 
 # Algorithmic per-cell demand of the fused batched map (the reference's
 # per-cell math; compensation not counted): FP32 flops (an FMA counts 2),
-# MUFU ops (sqrt, rcp, ex2), FP64 flops (D = AB - C^2 and the lnBtSG
-# accumulation).
+# MUFU ops (sqrt, rcp, ex2) and FP64 operations: D = AB - C^2 as two
+# (a multiply and a fused multiply-add) plus the lnBtSG accumulation as one
+# -- 3 operations per cell, the count the scope table fixes.  The measured
+# FP64 peak counts an FMA as 2 flops, so in consistent flop units the FP64
+# demand is 4 (mul 1 + fma 2 + add 1); the bench line states the fraction
+# both ways ("frac" with 3, "frac_fp64_flops" with 4).
 DEMAND = {1: {"fp32": 34.0, "mufu": 3.0, "fp64": 3.0},
           2: {"fp32": 55.0, "mufu": 3.0, "fp64": 3.0}}
+FP64_FLOPS_PER_CELL = 4.0
 KERNEL_WINDOW = {"rect_map_kernel": 1, "exp_map_kernel": 2}
 
 
 def profile_figure(kernel, key):
     """A "key = value" figure from the kernel's committed ncu summary."""
-    try:
-        with open(TRAFFIC_FILES[kernel]) as f:
-            for line in f:
-                if line.strip().startswith(key):
-                    return float(line.split("=")[1].split()[0])
-    except (OSError, ValueError, IndexError, KeyError):
-        pass
+    for line in profile_text(kernel).splitlines():
+        if line.strip().startswith(key):
+            try:
+                return float(line.split("=")[1].split()[0])
+            except (ValueError, IndexError):
+                return None
     return None
 
 
@@ -325,16 +406,25 @@ def roofline_block(batch, rect_ms, exp_ms, prefix_ms, fin_ms, peaks, clk, n_sms)
              "fp32_view": {"achieved_tflops": cps * d["fp32"] / 1e12,
                            "peak_tflops": peaks["fp32_tflops"],
                            "frac": cps * d["fp32"] / 1e12 / peaks["fp32_tflops"]}}
+        if bound == "fp64":
+            k["unit_note"] = ("achieved = 3 FP64 operations per cell (scope-table count: D as "
+                              "mul + fma, lnBtSG as add) x cells/s; peak = measured FP64 FMA "
+                              "rate with an FMA counted as 2 flops")
+            k["frac_fp64_flops"] = cps * FP64_FLOPS_PER_CELL / (peaks["fp64_tflops"] * 1e12)
+        current = profile_is_current(name)
+        k["profile_source_current"] = current
         ipc = profile_figure(name, "warp_instructions_per_cell")
         if ipc and clk and clk.get("sm_mhz"):
             issue = 4.0 * n_sms * clk["sm_mhz"] * 1e6 / ipc
             k["issue_view"] = {"warp_instructions_per_cell": ipc,
-                               "issue_bound_cells_per_s": issue, "frac": cps / issue}
+                               "issue_bound_cells_per_s": issue, "frac": cps / issue,
+                               "stale": not current}
         kernels[name] = k
     dom = max(kernels, key=lambda n: kernels[n]["ms"])
     d = kernels[dom]
     return {"bound": d["bound"], "achieved": d["achieved"], "peak": d["peak"],
             "unit": d["bound_unit"], "frac": d["frac"], "traffic": traffic_per_launch(dom),
+            "kernel_source_sha16": kernel_source_hash(),
             "achieved_cells_per_s": d["cells_per_s"], "roofline_cells_per_s": d["roofline_cells_per_s"],
             "kernel": dom, "kernels": kernels, "prefix_ms": prefix_ms, "finalize_ms": fin_ms,
             "peak_source": "FP32/FP64/MUFU of measured (tcw_probe_peaks on this GPU), HBM of "
@@ -350,17 +440,17 @@ def run_reference(args, ws, rank):
         return
     threads = os.cpu_count() or 1
     templates = workload(args.templates, args.seed)
-    for _ in range(args.warmup):
-        cpu_baseline(templates, min(2.0, args.cpu_seconds), threads)
-    vals, samples = [], []
+    for w in range(args.warmup):
+        cpu_baseline(templates, min(2.0, args.cpu_seconds), threads, seed=1000 + w)
+    vals, details = [], []
     t_all = time.perf_counter()
-    for _ in range(args.steps):
-        v, cells, used, dt = cpu_baseline(templates, args.cpu_seconds, threads)
+    for k in range(args.steps):
+        v, d = cpu_baseline(templates, args.cpu_seconds, threads, seed=2024 + k)
         vals.append(v)
-        samples.append((cells, used, dt))
+        details.append(d)
     elapsed = time.perf_counter() - t_all
     value = float(statistics.median(vals))
-    cells, used, dt = samples[-1]
+    d = details[-1]
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -368,9 +458,13 @@ def run_reference(args, ws, rank):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"batched {args.templates} templates, rect+exp, "
                    "SFTs 200-4000, 0-30% gaps, grids 256-2048^2",
-                   "sample": "consecutive templates per step (bounded CPU time)"},
+                   "sample": "each step: a different seeded stratified sample of the same "
+                             "workload, its time extrapolated to all templates"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{used} templates, {cells} cells, {dt:.1f} s per step"},
+                         "sample": d["sample"],
+                         "per_window_cells_per_s": d["per_window_cells_per_s"],
+                         "estimated_workload_s": d["estimated_workload_s"],
+                         "step_values": vals},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -527,14 +621,15 @@ def run_ours(args, ws, rank, local):
     cpu = None
     if not args.no_cpu_baseline and ws == 1:
         threads = os.cpu_count() or 1
-        v, cells, used, dt = cpu_baseline(templates, args.cpu_seconds, threads)
-        v1, cells1, used1, dt1 = cpu_baseline(templates, args.cpu_seconds / 3.0, 1)
+        v, d = cpu_baseline(templates, args.cpu_seconds, threads)
+        v1, d1 = cpu_baseline(templates, args.cpu_seconds / 3.0, 1)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"first {used} templates ({cells} cells, {dt:.1f} s), oracle port of "
-                         "the reference pycuda kernels' FP32 arithmetic + numpy reductions",
+               "sample": d["sample"] + "; oracle port of the reference pycuda kernels' FP32 "
+                         "arithmetic + numpy reductions",
+               "per_window_cells_per_s": d["per_window_cells_per_s"],
                "value_1thread": v1,
+               "sample_1thread": d1["sample"],
                "per_call_ms": cpu_per_call(threads),
-               "sample_1thread": f"first {used1} templates ({cells1} cells, {dt1:.1f} s)",
                "cpu": cpu_model()}
 
     line = {

@@ -105,6 +105,10 @@ const char *tcw_last_error(const tcw_handle *h);
 int tcw_device_count(int *count);
 int tcw_device_info(int device, char *name, size_t name_len, int *cc_major, int *cc_minor,
                     size_t *total_mem);
+/* Free and total device memory of `device` (cudaMemGetInfo; replaces the
+ * pycuda mem_get_info of _print_GPU_memory_MB, tcw:648-653).  The calling
+ * thread's current device is restored. */
+int tcw_device_memory(int device, size_t *free_bytes, size_t *total_bytes);
 
 /* Handle: owns a CUDA stream and a grow-only device workspace on `device`
  * (the pycuda context of tcw:419-470 and its per-call allocations,

@@ -80,6 +80,8 @@ SIGNATURES = {
                                        ctypes.POINTER(ctypes.c_int),
                                        ctypes.POINTER(ctypes.c_int),
                                        ctypes.POINTER(ctypes.c_size_t)]),
+    "tcw_device_memory": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_size_t),
+                                         ctypes.POINTER(ctypes.c_size_t)]),
     "tcw_create": (ctypes.c_int, [ctypes.POINTER(_vp), ctypes.c_int]),
     "tcw_destroy": (ctypes.c_int, [_vp]),
     "tcw_get_stream": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
@@ -186,6 +188,13 @@ def device_info(device):
     check(load().tcw_device_info(device, name, 256, ctypes.byref(major), ctypes.byref(minor),
                                  ctypes.byref(mem)))
     return dict(name=name.value.decode(), cc=(major.value, minor.value), total_mem=mem.value)
+
+
+def device_memory(device):
+    """(free, total) bytes of device memory."""
+    f, t = ctypes.c_size_t(0), ctypes.c_size_t(0)
+    check(load().tcw_device_memory(int(device), ctypes.byref(f), ctypes.byref(t)))
+    return f.value, t.value
 
 
 def probe_peaks(device=0):

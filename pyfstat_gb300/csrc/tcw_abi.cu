@@ -356,6 +356,29 @@ int tcw_device_info(int device, char *name, size_t name_len, int *cc_major, int 
   return TCW_OK;
 }
 
+int tcw_device_memory(int device, size_t *free_bytes, size_t *total_bytes) {
+  if (!free_bytes || !total_bytes) return TCW_ERR_INVALID_ARG;
+  int prev = -1;
+  if (cudaGetDevice(&prev) != cudaSuccess) {
+    cudaGetLastError();
+    return TCW_ERR_NO_DEVICE;
+  }
+  if (cudaSetDevice(device) != cudaSuccess) {
+    cudaGetLastError();
+    return TCW_ERR_NO_DEVICE;
+  }
+  size_t f = 0, t = 0;
+  const cudaError_t e = cudaMemGetInfo(&f, &t);
+  cudaSetDevice(prev);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return TCW_ERR_CUDA;
+  }
+  *free_bytes = f;
+  *total_bytes = t;
+  return TCW_OK;
+}
+
 int tcw_create(tcw_handle **out, int device) {
   if (!out) return TCW_ERR_INVALID_ARG;
   *out = nullptr;

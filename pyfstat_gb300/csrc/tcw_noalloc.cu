@@ -15,7 +15,12 @@
 //
 // Set-up: the first call on a device looks up the device address of the
 // array (cudaGetSymbolAddress, with that device current) and caches it per
-// device; make that first call before any stream capture.  All calls on a
+// device ordinal; make that first call before any stream capture.  The
+// cached address belongs to the runtime's primary context of that device:
+// after cudaDeviceReset of the device, or with another context made current
+// on it through the driver API, the array may live elsewhere and the cached
+// address is stale -- this entry point is for processes that keep the
+// primary context for their lifetime.  All calls on a
 // device share the array and it keeps the last call's contents, so calls
 // whose work overlaps on the GPU (different streams, or threads racing to the
 // same stream) corrupt each other's scratch: serialise them.  Everything a
@@ -130,7 +135,9 @@ extern "C" int tcw_map_plain_noalloc(void *stream, const float *d_atoms, uint32_
     uint32_t rows = (N_t0 + 15u) / 16u;
     rows = rows < 8u ? 8u : rows;
     rows_per_lane = rows < N_t0 ? rows : N_t0;
-    if (rows_per_lane > 65535u) return TCW_ERR_OVERFLOW;
+    // a lane's row chunk is a 16-bit count: longer columns become more row
+    // tiles, as in the handle-based entry point
+    if (rows_per_lane > 65535u) rows_per_lane = 65535u;
     rows_per_tile = rows_per_lane * (kBlock / tn);
   }
   const uint64_t n_mtiles = (N_t0 + rows_per_tile - 1u) / rows_per_tile;

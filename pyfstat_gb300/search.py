@@ -199,6 +199,14 @@ class TransientGridBatch:
         self.map_budget_cells = max(1, int(map_budget_bytes) // 4)
         self.bsgl = bsgl or (lambda twoF, twoFX: compute_log10BSGL(
             twoF, twoFX, Fstar0=Fstar0, oLGX=oLGX, use_log_correction=use_log_correction))
+        # provenance of the output columns: the maps, their reductions and the
+        # per-detector 2F follow the reference's algorithm and are checked
+        # against the FP64 oracle; the BSGL combination is a restatement of
+        # the published statistic that lalpulsar's ComputeBSGL implements,
+        # which is absent here, so its constants are not pinned to it
+        self.metadata = {"bsgl_parity": "unpinned" if bsgl is None else "caller-supplied",
+                         "bsgl": "Keitel et al. PRD 89 064023 (2014), Fstar0=%g" % Fstar0,
+                         "maps_parity": "FP64 oracle, 2F rel err <= 1e-5"}
 
     def output_keys(self):
         keys = ["twoF", "maxTwoF", "t0_ML", "tau_ML"]
@@ -342,4 +350,7 @@ def semicoherent_twoF(points, tboundaries, BSGL=False, detector_names=None, devi
         out["log10BSGL"] = np.where(np.isnan(l10), 0.0, l10)
         if detector_names is not None:
             out["detector_names"] = list(detector_names)
+        # the BSGL combination restates the published statistic; lalpulsar's
+        # ComputeBSGL is absent here, so its constants are not pinned to it
+        out["bsgl_parity"] = "unpinned" if bsgl is None else "caller-supplied"
     return out

@@ -238,6 +238,7 @@ def init_transient_fstat_map_features(feature="lal", cudaDeviceName=None):
             _current_context.detach()
         _current_context = B200Context(devnum)
         gpu_context = _current_context
+        _print_GPU_memory_MB("Available", devnum)
     elif feature == "pycuda":
         if not features["pycuda"]:
             raise RuntimeError("pycuda use was requested, but imports failed.")
@@ -283,6 +284,22 @@ def reshape_FstatAtomsVector(atomsVector):
     }
 
 
+def _print_GPU_memory_MB(key, device=None):
+    """Debug log of free / total device memory (tcw:648-653), at the same
+    points of a map computation as the reference logs it."""
+    if not logger.isEnabledFor(logging.DEBUG):
+        return
+    if device is None:
+        device = _current_context.device if _current_context is not None else 0
+    try:
+        free, total = _lib.device_memory(device)
+    except Exception as e:  # logging never fails a computation
+        logger.debug(f"{key} GPU memory: unavailable ({e})")
+        return
+    logger.debug("{} GPU memory: {:.4f} / {:.4f} MB free".format(
+        key, free / 2.0**20, total / 2.0**20))
+
+
 def _context():
     global _current_context
     if _current_context is None or _current_context.handle is None:
@@ -323,8 +340,11 @@ def b200_compute_transient_fstat_map(multiFstatAtoms, windowRange, BtSG=False):
             windowRange.type, TRANSIENT_NONE, TRANSIENT_LAST - 1))
     t0s, taus = expand_window_range(windowRange)
     flags = _lib.TCW_FLAG_LNBTSG | (_lib.TCW_FLAG_POSTERIORS if BtSG else 0)
-    F, res = _context().handle.map_plain_host(atoms, TAtom, t0_data, int(windowRange.type), t0s,
-                                              taus, want_map=True, flags=flags)
+    ctx = _context()
+    _print_GPU_memory_MB("Initial", ctx.device)
+    F, res = ctx.handle.map_plain_host(atoms, TAtom, t0_data, int(windowRange.type), t0s, taus,
+                                       want_map=True, flags=flags)
+    _print_GPU_memory_MB("Final", ctx.device)
     FstatMap.F_mn = F
     FstatMap.maxF = np.float32(res["maxF"])
     m, n = divmod(int(res["argmax"]), N_tau)

@@ -68,18 +68,29 @@ def hc_map(lib, c, comp=True, row_chunk=0):
     return F, ok.astype(bool)
 
 
-def argmax_ok(idx, F64, tol=REL_TOL):
+# How often argmax_ok / index_ok compared against a unique maximum (exact
+# index equality) and how often they took the tie branch, over the session;
+# conftest.py prints the counts at the end of the run.
+ARGMAX_COUNTS = {"unique": 0, "tie": 0}
+ARGMAX_TIE_LABELS = []
+
+
+def argmax_ok(idx, F64, tol=REL_TOL, label=None):
     """The flat argmax ``idx`` is the oracle's when the oracle's maximum is
     unique within the tolerance; where several cells tie within it (windows
-    holding the same atoms, e.g. one merged bin between gaps) any of them."""
+    holding the same atoms, e.g. one merged bin between gaps) any of them.
+    Each call is counted as a unique-maximum or a tie-branch comparison."""
     F64 = np.asarray(F64, dtype=np.float64).reshape(-1)
     top = F64.max()
     tied = np.flatnonzero(F64 >= top - 2 * tol * abs(top))
     if tied.size == 1:
+        ARGMAX_COUNTS["unique"] += 1
         return int(idx) == int(tied[0])
+    ARGMAX_COUNTS["tie"] += 1
+    ARGMAX_TIE_LABELS.append(f"{label or '?'} ({tied.size} cells)")
     return int(idx) in set(int(i) for i in tied)
 
 
-def index_ok(idx, values, tol=REL_TOL):
+def index_ok(idx, values, tol=REL_TOL, label=None):
     """Same rule for the argmax of a 1-D marginal (posterior row/column sums)."""
-    return argmax_ok(idx, values, tol)
+    return argmax_ok(idx, values, tol, label)

@@ -13,6 +13,20 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
 
 
+def pytest_terminal_summary(terminalreporter):
+    """Reports how many argmax / posterior-index comparisons had a unique
+    maximum (exact index equality) and how many took the tie branch."""
+    mod = sys.modules.get("_helpers")
+    if mod is None:
+        return
+    c = mod.ARGMAX_COUNTS
+    if c["unique"] or c["tie"]:
+        terminalreporter.write_line(
+            f"argmax comparisons: {c['unique']} unique maximum (exact index), "
+            f"{c['tie']} tie branch" +
+            (f" [{'; '.join(mod.ARGMAX_TIE_LABELS[:20])}]" if c["tie"] else ""))
+
+
 @pytest.fixture(scope="session")
 def oracle():
     import oracle as O

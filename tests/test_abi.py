@@ -59,7 +59,11 @@ def test_calls_without_a_gpu(lib):
     assert b"unknown" in lib.tcw_strerror(-99)
     assert lib.tcw_destroy(None) == _lib.TCW_ERR_INVALID_ARG
     assert lib.tcw_sync(None, 0) == _lib.TCW_ERR_INVALID_ARG
+    f, t = ctypes.c_size_t(), ctypes.c_size_t()
+    assert lib.tcw_device_memory(0, None, ctypes.byref(t)) == _lib.TCW_ERR_INVALID_ARG
     if _lib.device_count() == 0:
+        assert lib.tcw_device_memory(0, ctypes.byref(f), ctypes.byref(t)) == \
+            _lib.TCW_ERR_NO_DEVICE
         h = ctypes.c_void_p()
         assert lib.tcw_create(ctypes.byref(h), 0) == _lib.TCW_ERR_NO_DEVICE
         assert not h.value

@@ -122,22 +122,45 @@ def test_gradients_match_central_finite_differences(torch_cuda):
             assert float(ga_s[row + i, ch]) == pytest.approx(fs, rel=1e-4, abs=1e-6)
 
 
-def test_differentiation_workload_256x2000x1024sq(torch_cuda):
-    """256 templates, 2000 SFTs x 2 detectors, 1024 x 1024 (t0, tau): forward
-    and backward run; tau gradients of a few templates against central FP64
-    finite differences of the GPU forward: d softmax2F / d tau_min (at
-    T = 0.1 the soft-max sits on its largest cells, whose tau moves with
-    tau_min) and d lnBtSG / d tau_max (a sum over all cells)."""
-    torch = torch_cuda
-    from pyfstat_gb300.autograd import ExpDiffBatch
-
+def _config3_templates(tau_min):
+    """256 templates, 2000 SFTs x 2 detectors, 1024 t0 x 3600 s (~ the 2000-SFT
+    span) x 1024 tau from ``tau_min`` in steps of 1200 s (boundary-safe grids,
+    see templates_small: 3 tau_min = 225 mod 900)."""
     tl = []
     for k in range(256):
         t0_data, A = synth.merged_atoms(5000 + k, 2000, 2)
-        # 1024 t0 x 3600 s ~ the 2000-SFT span; tau in [1875 s, ~span/3] in
-        # steps of 1200 s (boundary-safe grids, see templates_small)
         tl.append(dict(atoms=A, TAtom=1800, t0_data=t0_data, t0=t0_data + 450, dt0=3600,
-                       N_t0=1024, N_tau=1024, tau_min=1875.0, tau_max=1875.0 + 1200.0 * 1023))
+                       N_t0=1024, N_tau=1024, tau_min=tau_min, tau_max=tau_min + 1200.0 * 1023))
+    return tl
+
+
+def _fp32_step(x, h):
+    """Central-difference points around the FP32 value x: (x - h', x + h'')
+    as FP32 values and their exact FP64 distance."""
+    lo = np.float32(np.float64(x) - h)
+    hi = np.float32(np.float64(x) + h)
+    return lo, hi, float(np.float64(hi) - np.float64(lo))
+
+
+@pytest.mark.parametrize("grid", ["short_tau", "interior_tau"])
+def test_differentiation_workload_256x2000x1024sq(torch_cuda, grid):
+    """256 templates, 2000 SFTs x 2 detectors, 1024 x 1024 (t0, tau): forward
+    and backward of all templates; for 3 of them, every gradient against
+    central FP64 finite differences of the GPU's FP64 forward (bar 1e-4
+    relative): d/d tau_min, d/d tau_max and d/d atom for 8 atoms x all 7
+    channels (the 4 atoms with the largest adjoint and 4 random ones).
+
+    Two tau grids on the same atoms: "short_tau" starts at 1875 s, where
+    windows of a few SFTs are near-singular and their huge F puts the weight
+    of both statistics in the first tau column (so the tau_min derivatives
+    carry it and the tau_max ones nearly vanish); "interior_tau" starts at
+    30075 s (windows of >= 50 SFTs, well conditioned), so the weight lies in
+    interior tau columns and d/d tau_max is non-zero for both statistics."""
+    torch = torch_cuda
+    from pyfstat_gb300.autograd import ExpDiffBatch
+
+    tau_min0 = 1875.0 if grid == "short_tau" else 30075.0
+    tl = _config3_templates(tau_min0)
     batch = ExpDiffBatch(tl, temperature=0.1)
     dev = torch.device("cuda:0")
     atoms = torch.from_numpy(batch.atoms).to(dev)
@@ -150,39 +173,100 @@ def test_differentiation_workload_256x2000x1024sq(torch_cuda):
     t1 = time.perf_counter()
     one = torch.ones(256, dtype=torch.float64, device=dev)
     zero = torch.zeros(256, dtype=torch.float64, device=dev)
-    ga, gt_s = batch.backward_raw(atoms, tmin, tmax, lnB, soft, zero, one)
+    ga_s, gt_s = batch.backward_raw(atoms, tmin, tmax, lnB, soft, zero, one)
     torch.cuda.synchronize()
     t2 = time.perf_counter()
-    _, gt_l = batch.backward_raw(atoms, tmin, tmax, lnB, soft, one, zero)
+    ga_l, gt_l = batch.backward_raw(atoms, tmin, tmax, lnB, soft, one, zero)
     torch.cuda.synchronize()
-    print(f"\n256 templates x 2000 SFTs x 2 detectors, 1024 x 1024: forward "
+    print(f"\n[{grid}] 256 templates x 2000 SFTs x 2 detectors, 1024 x 1024: forward "
           f"{1e3 * (t1 - t0):.1f} ms, backward {1e3 * (t2 - t1):.1f} ms for "
           f"{256 * 1024 * 1024:.3g} cells")
-    assert torch.isfinite(ga).all() and torch.isfinite(gt_s).all()
-    for k in (0, 17, 255):
-        # tau_min moves by ~2 s and tau_max by ~1.2 s: no window boundary moves.
-        # The cells that carry weight in both statistics lie in the first tau
-        # column here, so the tau_min derivatives are the informative ones;
-        # the tau_max ones are checked too (they may vanish).
-        fd = {}
-        for which, base, hh in (("min", tmin, 1e-3 * tmin[k]), ("max", tmax, 1e-6 * tmax[k])):
-            p, m = base.copy(), base.copy()
-            p[k] += hh
-            m[k] -= hh
-            args_p = (p, tmax) if which == "min" else (tmin, p)
-            args_m = (m, tmax) if which == "min" else (tmin, m)
-            lp, sp = batch.forward_raw(atoms, *args_p)
-            lm, sm = batch.forward_raw(atoms, *args_m)
-            fd[which] = ((float(lp[k]) - float(lm[k])) / (2 * hh),
-                         (float(sp[k]) - float(sm[k])) / (2 * hh))
-        print(f"template {k}: tau_min: d lnBtSG adjoint {float(gt_l[k, 0]):.9e} FD "
-              f"{fd['min'][0]:.9e}, d softmax2F adjoint {float(gt_s[k, 0]):.9e} FD "
-              f"{fd['min'][1]:.9e}; tau_max: d lnBtSG {float(gt_l[k, 1]):.3e} / {fd['max'][0]:.3e}")
-        assert fd["min"][0] != 0.0 and fd["min"][1] != 0.0
-        assert fd["min"][0] == pytest.approx(float(gt_l[k, 0]), rel=1e-4)
-        assert fd["min"][1] == pytest.approx(float(gt_s[k, 0]), rel=1e-4)
-        assert fd["max"][0] == pytest.approx(float(gt_l[k, 1]), rel=1e-4, abs=1e-12)
-        assert fd["max"][1] == pytest.approx(float(gt_s[k, 1]), rel=1e-4, abs=1e-12)
+    assert torch.isfinite(ga_s).all() and torch.isfinite(ga_l).all()
+    assert torch.isfinite(gt_s).all() and torch.isfinite(gt_l).all()
+    ga_s, ga_l = ga_s.cpu().numpy(), ga_l.cpu().numpy()
+
+    # finite differences on a batch of the 3 checked templates (independent
+    # of the others, so its forward gives the same values)
+    ks = (0, 17, 255)
+    sub = ExpDiffBatch([tl[k] for k in ks], temperature=0.1, handle=batch.handle)
+    s_atoms = torch.from_numpy(sub.atoms).to(dev)
+    s_min, s_max = tmin[list(ks)], tmax[list(ks)]
+    l0, s0 = sub.forward_raw(s_atoms, s_min, s_max)
+    for j, k in enumerate(ks):
+        assert float(l0[j]) == pytest.approx(float(lnB[k]), rel=1e-12)
+        assert float(s0[j]) == pytest.approx(float(soft[k]), rel=1e-12)
+
+    # tau: tau_min moves by ~2 s (short) / 1e-5 relative, tau_max by ~1.2 s,
+    # so no window boundary moves
+    for which, base, rel_h in (("min", s_min, 1e-3 if grid == "short_tau" else 3e-5),
+                               ("max", s_max, 1e-6)):
+        hh = rel_h * base
+        args_p = (s_min + hh, s_max) if which == "min" else (s_min, s_max + hh)
+        args_m = (s_min - hh, s_max) if which == "min" else (s_min, s_max - hh)
+        lp, sp = sub.forward_raw(s_atoms, *args_p)
+        lm, sm = sub.forward_raw(s_atoms, *args_m)
+        col = 0 if which == "min" else 1
+        for j, k in enumerate(ks):
+            fd_l = (float(lp[j]) - float(lm[j])) / (2 * hh[j])
+            fd_s = (float(sp[j]) - float(sm[j])) / (2 * hh[j])
+            print(f"template {k}: d/dtau_{which}: lnBtSG adjoint {float(gt_l[k, col]):.9e} "
+                  f"FD {fd_l:.9e}; softmax2F adjoint {float(gt_s[k, col]):.9e} FD {fd_s:.9e}")
+            informative = which == "min" or grid == "interior_tau"
+            if informative:
+                # non-vacuous: both sides are clearly non-zero
+                assert abs(fd_l) > 1e-9 and abs(fd_s) > 1e-9, (which, k, fd_l, fd_s)
+                assert fd_l == pytest.approx(float(gt_l[k, col]), rel=1e-4)
+                assert fd_s == pytest.approx(float(gt_s[k, col]), rel=1e-4)
+            else:
+                # the weight sits in the first column: the derivative nearly
+                # vanishes; adjoint and FD still agree to 1e-4 of the tau_min one
+                scale_l, scale_s = abs(float(gt_l[k, 0])), abs(float(gt_s[k, 0]))
+                assert abs(fd_l - float(gt_l[k, col])) <= 1e-4 * max(abs(fd_l), scale_l)
+                assert abs(fd_s - float(gt_s[k, col])) <= 1e-4 * max(abs(fd_s), scale_s)
+
+    # atoms: 8 atoms per template x 7 channels; the same (atom, channel) slot is
+    # perturbed in all 3 templates at once (their results are independent)
+    rng = np.random.default_rng(3)
+    picks, rows = [], []
+    for j, k in enumerate(ks):
+        r0 = int(batch.desc["atom_offset"][k])
+        n = int(batch.desc["numAtoms"][k])
+        mag = np.abs(ga_s[r0:r0 + n]).sum(axis=1) + np.abs(ga_l[r0:r0 + n]).sum(axis=1)
+        top = list(np.argsort(mag)[-4:][::-1])
+        rest = [int(i) for i in rng.permutation(np.flatnonzero(mag > 0)) if i not in top][:4]
+        picks.append([int(i) for i in top] + rest)
+        rows.append((r0, int(sub.desc["atom_offset"][j])))
+    base = sub.atoms.copy()
+    checked = 0
+    for slot in range(8):
+        for ch in range(7):
+            xp, xm, steps = base.copy(), base.copy(), []
+            for j in range(3):
+                i = picks[j][slot]
+                x = base[rows[j][1] + i, ch]
+                # a few dozen FP32 ulps: small enough for the truncation error
+                # of cells near the conditioning cut (F up to ~1e4, strongly
+                # non-linear in the atoms), large enough for FP64 round-off
+                h = 2e-6 * abs(float(x)) if x != 0 else 1e-9
+                lo, hi, step = _fp32_step(x, h)
+                xm[rows[j][1] + i, ch] = lo
+                xp[rows[j][1] + i, ch] = hi
+                steps.append(step)
+            lp, sp = sub.forward_raw(torch.from_numpy(xp).to(dev), s_min, s_max)
+            lm, sm = sub.forward_raw(torch.from_numpy(xm).to(dev), s_min, s_max)
+            lp, sp, lm, sm = (v.cpu().numpy() for v in (lp, sp, lm, sm))
+            for j, k in enumerate(ks):
+                i = picks[j][slot]
+                r0 = rows[j][0]
+                n = int(batch.desc["numAtoms"][k])
+                for fd, g in (((lp[j] - lm[j]) / steps[j], ga_l[r0:r0 + n]),
+                              ((sp[j] - sm[j]) / steps[j], ga_s[r0:r0 + n])):
+                    scale = np.abs(g).max()
+                    assert float(g[i, ch]) == pytest.approx(float(fd), rel=1e-4,
+                                                           abs=1e-6 * scale), (k, i, ch)
+                    checked += 1
+    print(f"[{grid}] atom gradients checked against FP64 finite differences: {checked} "
+          f"(3 templates x 8 atoms x 7 channels x 2 statistics)")
 
 
 def test_rect_and_exp_templates_in_one_batch(torch_cuda):

@@ -42,22 +42,23 @@ def _check_case(handle, oracle, c, flags=FLAGS_ALL, tol=REL_TOL):
     assert float(res["maxF"]) == float(F.max())
     assert int(res["argmax"]) == int(np.argmax(F))
     if nband == 0:
-        assert argmax_ok(res["argmax"], F64), c.get("name")
+        name = c.get("name")
+        assert argmax_ok(res["argmax"], F64, label=f"{name} argmax"), name
         lnB64 = oracle.lnBtSG(F64)
         assert float(res["lnBtSG"]) == pytest.approx(lnB64, rel=tol, abs=1e-6)
         if flags & 0x2:
             e = np.exp(F64 - F64.max())
-            assert index_ok(res["t0_mp_idx"], e.sum(axis=1)), c.get("name")
-            assert index_ok(res["tau_mp_idx"], e.sum(axis=0)), c.get("name")
+            assert index_ok(res["t0_mp_idx"], e.sum(axis=1), label=f"{name} t0_MP"), name
+            assert index_ok(res["tau_mp_idx"], e.sum(axis=0), label=f"{name} tau_MP"), name
     return F, res
 
 
 def test_rect_workload_480(handle, oracle):
-    _check_case(handle, oracle, synth.plain_rect_case())
+    _check_case(handle, oracle, dict(synth.plain_rect_case(), name="rect480"))
 
 
 def test_exp_workload_480x512_log_tau(handle, oracle):
-    _check_case(handle, oracle, synth.plain_exp_case())
+    _check_case(handle, oracle, dict(synth.plain_exp_case(), name="exp480x512log"))
 
 
 def test_golden_edge_cases(handle, oracle, golden):

@@ -152,3 +152,14 @@ def test_b200_feature_requires_compute_capability_10_3(monkeypatch, cc, expect):
     if not expect:
         with pytest.raises(RuntimeError, match="compute capability 10.3"):
             tcw.init_transient_fstat_map_features("b200")
+
+
+def test_gpu_memory_debug_log_never_fails_the_call(caplog):
+    # the reference logs free / total device memory at debug level around each
+    # map (_print_GPU_memory_MB, tcw:648-653); without a device the line says
+    # so instead of raising
+    import logging
+
+    with caplog.at_level(logging.DEBUG, logger=tcw.logger.name):
+        tcw._print_GPU_memory_MB("Initial", 0)
+    assert any("Initial GPU memory" in r.getMessage() for r in caplog.records)
