@@ -48,14 +48,18 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=12.0,
                    help="target CPU time of the bounded CPU-baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-grad", action="store_true",
+                   help="skip the differentiation workload (forward/backward timing)")
     p.add_argument("--plain-templates", type=int, default=256,
                    help="templates timed with the plain per-template kernel")
     p.add_argument("--window", choices=["both", "rect", "exp"], default="both",
                    help="restrict the workload to one window type (breakdown runs)")
-    p.add_argument("--case", choices=["plain-rect", "plain-exp"], default=None,
+    p.add_argument("--case", choices=["plain-rect", "plain-exp", "single-480"], default=None,
                    help="instead of the benchmark: time one single-template map with the map "
                         "written (8192 t0 x 4096 tau over one year of two-detector data; the "
-                        "134 MB map exceeds L2), for the memory-side profile of the plain kernel")
+                        "134 MB map exceeds L2), for the memory-side profile of the plain kernel; "
+                        "single-480: the 480 x 480 rect and 480 x 512 log-tau exp single-template "
+                        "maps on device buffers (--steps calls each)")
     p.add_argument("--tile", type=str, default="auto",
                    help="tile config as JSON, 'auto' for the autotuner (default), "
                         "'default' for the library defaults")
@@ -249,6 +253,106 @@ def dropin_per_call(h, reps=20):
                                                 c["t0s"], c["taus"], want_map=True, flags=flags))
     return {"rect_480x480_dispatcher_ms": rect_ms, "exp_480x512log_c_abi_ms": exp_ms,
             "note": "median of 20 calls, full F map and result back on the host"}
+
+
+def plain_configs(h, dev, torch, stream, hbm, reps=200):
+    """The single-template workloads on device buffers (map written, lnBtSG
+    and posteriors), timed with CUDA events over ``reps`` calls: the 480 x 480
+    rectangular map of one 480-SFT detector and the 480 t0 x 512 log-spaced
+    tau exponential map of two merged detectors.  HBM figures use the
+    algorithmic bytes: 28 B per atom read + 4 B per map cell written."""
+    from pyfstat_gb300 import _lib, synth
+
+    out = {}
+    for name, c in (("rect_480x480", synth.plain_rect_case()),
+                    ("exp_480x512log", synth.plain_exp_case())):
+        A = torch.from_numpy(c["atoms"]).to(dev)
+        t0s = torch.from_numpy(c["t0s"].view(np.int32)).to(dev)
+        taus = torch.from_numpy(c["taus"].view(np.int32)).to(dev)
+        N_t0, N_tau = len(c["t0s"]), len(c["taus"])
+        F = torch.empty((N_t0, N_tau), dtype=torch.float32, device=dev)
+        r = torch.zeros(5, dtype=torch.float64, device=dev)
+        flags = _lib.TCW_FLAG_LNBTSG | _lib.TCW_FLAG_POSTERIORS
+
+        def call():
+            h.map_plain(A, A.shape[0], c["TAtom"], c["t0_data"], c["window"], t0s, N_t0, taus,
+                        N_tau, F, r, flags=flags)
+
+        for _ in range(min(10, reps)):
+            call()
+        torch.cuda.synchronize(dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            call()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / reps
+        cells = N_t0 * N_tau
+        nbytes = 28.0 * A.shape[0] + 4.0 * cells
+        gbs = nbytes / (ms * 1e-3) / 1e9
+        out[name] = {"ms_per_call": ms, "cells_per_s": cells / (ms * 1e-3),
+                     "algorithmic_bytes": nbytes, "hbm_gbs": gbs,
+                     "frac_of_hbm": gbs / hbm if hbm else None,
+                     "note": "device buffers, map written, lnBtSG and posteriors; all "
+                             "launches of one call (map, finalize, posteriors) in the time"}
+    return out
+
+
+# Algorithmic FP64 work per cell of the differentiable statistics: the
+# forward pass is the map's per-cell math (55 flops with an FMA as 2) in
+# FP64; the backward pass recomputes the window sums and runs their adjoint
+# (twice the forward).
+GRAD_FP64_FLOPS = {"forward": 55.0, "backward": 110.0}
+
+
+def grad_case(torch, dev, peaks, reps=3):
+    """Differentiation workload: 256 templates x 2000 SFTs x 2 detectors,
+    exponential windows, 1024 t0 x 1024 tau; forward (lnBtSG and soft-max 2F)
+    and backward (gradients of both w.r.t. atoms and tau), CUDA events."""
+    from pyfstat_gb300 import synth
+    from pyfstat_gb300.autograd import DiffBatch
+
+    tl = []
+    for k in range(256):
+        t0_data, A = synth.merged_atoms(5000 + k, 2000, 2)
+        tl.append(dict(atoms=A, TAtom=1800, t0_data=t0_data, t0=t0_data + 450, dt0=3600,
+                       N_t0=1024, N_tau=1024, tau_min=30075.0,
+                       tau_max=30075.0 + 1200.0 * 1023))
+    b = DiffBatch(tl, device=dev.index, temperature=0.1)
+    atoms = torch.from_numpy(b.atoms).to(dev)
+    tmin = np.array([t["tau_min"] for t in tl])
+    tmax = np.array([t["tau_max"] for t in tl])
+    one = torch.ones(256, dtype=torch.float64, device=dev)
+    lnB, soft = b.forward_raw(atoms, tmin, tmax)
+    b.backward_raw(atoms, tmin, tmax, lnB, soft, one, one)
+    torch.cuda.synchronize(dev)
+    s = torch.cuda.current_stream(dev)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    fwd, bwd = [], []
+    for _ in range(reps):
+        ev[0].record(s)
+        lnB, soft = b.forward_raw(atoms, tmin, tmax)
+        ev[1].record(s)
+        b.backward_raw(atoms, tmin, tmax, lnB, soft, one, one)
+        ev[2].record(s)
+        torch.cuda.synchronize(dev)
+        fwd.append(ev[0].elapsed_time(ev[1]))
+        bwd.append(ev[1].elapsed_time(ev[2]))
+    cells = 256 * 1024 * 1024
+    out = {"workload": "256 templates x 2000 SFTs x 2 detectors (exp), 1024 t0 x 1024 tau "
+                       "(tau from 30075 s in steps of 1200 s), temperature 0.1",
+           "cells": cells}
+    for name, ms in (("forward", statistics.median(fwd)), ("backward", statistics.median(bwd))):
+        cps = cells / (ms * 1e-3)
+        ach = cps * GRAD_FP64_FLOPS[name] / 1e12
+        out[name] = {"ms": ms, "cells_per_s": cps,
+                     "roofline": {"bound": "fp64", "achieved": ach,
+                                  "peak": peaks["fp64_tflops"], "unit": "TFLOP/s",
+                                  "frac": ach / peaks["fp64_tflops"],
+                                  "fp64_flops_per_cell": GRAD_FP64_FLOPS[name]}}
+    return out
 
 
 def cpu_per_call(threads, reps=3):
@@ -613,6 +717,14 @@ def run_ours(args, ws, rank, local):
                         "error-free FP32 products of the default path"}
     per_call = dropin_per_call(h)
     peaks = _lib.probe_peaks(dev.index)
+    hbm_peak = None
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            hbm_peak = json.load(f).get("hbm_gbs")
+    except (OSError, ValueError):
+        pass
+    single = plain_configs(h, dev, torch, stream, hbm_peak)
+    grad = grad_case(torch, dev, peaks) if not args.no_grad else None
     roofline = roofline_block(batch, rect_ms, exp_ms, prefix_ms, fin_ms, peaks, clk,
                               torch.cuda.get_device_properties(dev).multi_processor_count)
     n_rect = int(np.sum(batch.desc["window"] == 1))
@@ -655,6 +767,8 @@ def run_ours(args, ws, rank, local):
         "plain_per_template": plain,
         "fp64_determinant_variant": fp64_det,
         "dropin_per_call": per_call,
+        "single_template_device": single,
+        "grad": grad,
         "gpu_launches": launches_per_step(n_rect, n_t - n_rect) * args.steps,
         "clocks": clk,
     }
@@ -716,9 +830,36 @@ def run_case(args):
     h.close()
 
 
+def run_single_480(args):
+    """The two single-template workloads alone (for their ncu captures)."""
+    import torch
+
+    from pyfstat_gb300 import _lib
+
+    dev = torch.device("cuda", 0)
+    h = _lib.Handle(0)
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    h.set_stream(stream.cuda_stream)
+    hbm = None
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            hbm = json.load(f).get("hbm_gbs")
+    except (OSError, ValueError):
+        pass
+    print(json.dumps({"case": "single-480",
+                      **plain_configs(h, dev, torch, stream, hbm, reps=max(1, args.steps))}),
+          flush=True)
+    h.close()
+
+
 def main():
     args = parse()
     ws, rank, local = dist_env()
+    if args.case == "single-480":
+        if rank == 0:
+            run_single_480(args)
+        return
     if args.case:
         if rank == 0:
             run_case(args)

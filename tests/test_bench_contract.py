@@ -64,6 +64,14 @@ def test_gpu_arm_line():
     assert d["gpu_launches"] >= 2 * 5
     c = d["clocks"]
     assert "sm_mhz" in c and "sm_max_mhz" in c and isinstance(c["reasons"], list)
+    for name in ("rect_480x480", "exp_480x512log"):
+        s = d["single_template_device"][name]
+        assert s["cells_per_s"] > 0 and s["hbm_gbs"] > 0
+    g = d["grad"]
+    for name in ("forward", "backward"):
+        assert g[name]["ms"] > 0 and g[name]["roofline"]["bound"] == "fp64"
+        assert 0 < g[name]["roofline"]["frac"] < 2
+    assert isinstance(r["kernels"][r["kernel"]]["profile_source_current"], bool)
 
 
 @pytest.mark.gpu
