@@ -89,7 +89,8 @@ typedef struct {
 typedef struct {
   uint32_t rect_tn;       /* columns per rect tile (any >= 1) */
   uint32_t rect_tm;       /* rows per rect tile: 32, 64 or 128 (one thread per row) */
-  uint32_t exp_tn;        /* columns per exp block: 32, 64 or 128 */
+  uint32_t exp_tn;        /* columns per exp block: 32, 64 or 128 (single-template
+                             calls; batched plans run 32-column warp tiles) */
   uint32_t exp_rows;      /* rows per exp thread chunk (0 = whole column) */
   uint32_t blocks_per_sm; /* cap on persistent blocks per SM (occupancy limits it too) */
 } tcw_tile_config;

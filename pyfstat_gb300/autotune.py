@@ -20,7 +20,9 @@ import numpy as np
 from . import _lib
 
 RECT_CANDIDATES = [(tm, tn) for tm in (32, 64, 128) for tn in (32, 64, 128, 256)]
-EXP_CANDIDATES = [(tn, rows) for tn in (32, 64, 128) for rows in (0, 64, 256)]
+# batched plans run exponential tiles as 32-column warp tiles: only the rows
+# per tile (0 = whole columns) are tuned
+EXP_CANDIDATES = [(32, rows) for rows in (0, 64, 256, 1024)]
 
 
 def cache_path():

@@ -209,9 +209,12 @@ int prec_of(int flags) {
 
 // Tiles of one template.  Rect: tn columns x tm rows per block.  Exp: tn
 // columns per block, each thread one column over `rows` rows, the block's
-// 128/tn thread rows covering consecutive row chunks.
+// 128/tn thread rows covering consecutive row chunks; with `warp_tiles`
+// (persistent plans, whose exp kernel schedules by warp) 32 columns over
+// `rows` rows per tile.
 void tile_template(uint32_t tmpl, const TemplateDev &t, const tcw_tile_config &cfg,
-                   std::vector<WorkItem> &items, std::vector<double> *cost) {
+                   std::vector<WorkItem> &items, std::vector<double> *cost,
+                   bool warp_tiles = false) {
   const uint32_t N_t0 = t.N_t0, N_tau = t.N_tau;
   if (t.window == TCW_WINDOW_RECT) {
     const uint32_t tn = cfg.rect_tn, tm = cfg.rect_tm;
@@ -229,7 +232,7 @@ void tile_template(uint32_t tmpl, const TemplateDev &t, const tcw_tile_config &c
         if (cost) cost->push_back((double)(w.m1 - w.m0) * (w.n1 - w.n0));
       }
   } else {
-    const uint32_t tn = cfg.exp_tn, lanes = kBlock / tn;
+    const uint32_t tn = warp_tiles ? 32u : cfg.exp_tn, lanes = warp_tiles ? 1u : kBlock / tn;
     uint32_t rows = cfg.exp_rows ? cfg.exp_rows : N_t0;
     // a lane's row chunk is a 16-bit count: longer columns become several tiles
     rows = std::min(std::min(rows, N_t0), 65535u);
@@ -727,6 +730,7 @@ int tcw_plan_create(tcw_handle *h, const tcw_template_desc *desc, uint32_t n_tem
   tcw_tile_config cfg{};
   if (cfg_in) cfg = *cfg_in;
   fill_cfg_defaults(cfg);
+  cfg.exp_tn = 32;  // plans run 32-column warp tiles (tile_template's warp_tiles)
 
   tcw_plan *p = new (std::nothrow) tcw_plan();
   if (!p) return TCW_ERR_ALLOC;
@@ -787,7 +791,7 @@ int tcw_plan_create(tcw_handle *h, const tcw_template_desc *desc, uint32_t n_tem
       atom_rows = std::max<uint64_t>(atom_rows, d.atom_offset + d.numAtoms);
       cells += (uint64_t)d.N_t0 * d.N_tau;
       const size_t first = items.size();
-      tile_template(k, t, cfg, items, &cost);
+      tile_template(k, t, cfg, items, &cost, true);
       t.part_off = (uint32_t)first;
       t.n_parts = (uint32_t)(items.size() - first);
       for (size_t i = first; i < items.size(); i++) items[i].part = (uint32_t)i;
@@ -1072,9 +1076,9 @@ int tcw_plan_run_timed(tcw_handle *h, tcw_plan *p, const float *d_atoms, tcw_res
 // Validates descriptors, uploads descriptors, tiles and grids into the
 // handle's workspace; returns the layout of what follows them.
 struct DiffSetup {
-  size_t o_T, o_items, o_parts, o_t0, o_cnt, o_scratch, o_rlist, o_D64, total;
+  size_t o_T, o_items, o_parts, o_t0, o_cnt, o_scratch, o_rlist, o_D64, o_elist, o_A8, total;
   uint32_t n_items, n_blocks, max_rows;
-  uint32_t n_rect_items, n_rect_blocks, n_rect;
+  uint32_t n_rect_items, n_rect_blocks, n_rect, n_exp;
   uint64_t p_rows;
 };
 
@@ -1083,9 +1087,9 @@ static int diff_prepare(tcw_handle *h, const tcw_diff_desc *desc, uint32_t n,
   if (!desc || n == 0 || !t0s) return set_err(h, TCW_ERR_INVALID_ARG, "empty template list");
   std::vector<DiffTemplate> T(n);
   std::vector<DiffItem> items, ritems;
-  std::vector<uint32_t> rlist;
+  std::vector<uint32_t> rlist, elist;
   uint32_t max_rows = 0;
-  uint64_t p_rows = 0;
+  uint64_t p_rows = 0, atom_rows = 0;
   try {
     for (uint32_t k = 0; k < n; k++) {
       const tcw_diff_desc &d = desc[k];
@@ -1129,6 +1133,8 @@ static int diff_prepare(tcw_handle *h, const tcw_diff_desc *desc, uint32_t n,
         rlist.push_back(k);
       } else {
         max_rows = std::max(max_rows, d.N_t0);
+        elist.push_back(k);
+        atom_rows = std::max<uint64_t>(atom_rows, d.atom_offset + d.numAtoms);
       }
       T[k] = t;
     }
@@ -1143,6 +1149,7 @@ static int diff_prepare(tcw_handle *h, const tcw_diff_desc *desc, uint32_t n,
   }
   S.max_rows = max_rows;
   S.n_rect = (uint32_t)rlist.size();
+  S.n_exp = (uint32_t)elist.size();
   S.p_rows = p_rows;
   S.n_blocks = (uint32_t)std::max<uint64_t>(
       1, std::min<uint64_t>(S.n_items, (uint64_t)diff_blocks_per_sm(pass) * h->n_sms));
@@ -1155,12 +1162,16 @@ static int diff_prepare(tcw_handle *h, const tcw_diff_desc *desc, uint32_t n,
   S.o_t0 = L.add(sizeof(uint32_t) * n_t0s);
   S.o_cnt = L.add(2 * sizeof(uint32_t));
   S.o_rlist = L.add(sizeof(uint32_t) * std::max<size_t>(1, rlist.size()));
+  S.o_elist = L.add(sizeof(uint32_t) * std::max<size_t>(1, elist.size()));
   const size_t ctl = L.total;
   S.o_parts = L.add(sizeof(DiffPartial) * n_all_items);
   S.o_scratch = (pass == 1 && S.n_items)
                     ? L.add(sizeof(float) * TCW_DIFF_SLOTS * 128u * (size_t)max_rows * S.n_blocks)
                     : 0;
   S.o_D64 = pass == 1 ? L.add(sizeof(double) * 8u * std::max<uint64_t>(1, p_rows)) : 0;
+  // forward: the exponential templates' atoms in 32-byte rows, at their own row index
+  S.o_A8 = (pass == 0 && S.n_items) ? L.add(sizeof(float) * 8u * std::max<uint64_t>(1, atom_rows))
+                                    : 0;
   S.total = L.total;
   int rc = ensure_ws(h, S.total);
   if (rc) return rc;
@@ -1171,6 +1182,7 @@ static int diff_prepare(tcw_handle *h, const tcw_diff_desc *desc, uint32_t n,
   memcpy(h->h_stage + S.o_t0, t0s, sizeof(uint32_t) * n_t0s);
   memset(h->h_stage + S.o_cnt, 0, 2 * sizeof(uint32_t));
   if (!rlist.empty()) memcpy(h->h_stage + S.o_rlist, rlist.data(), sizeof(uint32_t) * rlist.size());
+  if (!elist.empty()) memcpy(h->h_stage + S.o_elist, elist.data(), sizeof(uint32_t) * elist.size());
   TCW_CUDA(h, cudaMemcpyAsync(h->d_ws, h->h_stage, ctl, cudaMemcpyHostToDevice, h->stream));
   TCW_CUDA(h, cudaEventRecord(h->stage_ev, h->stream));
   h->stage_pending = true;
@@ -1196,6 +1208,9 @@ static DiffLaunch diff_launch(tcw_handle *h, const DiffSetup &S, const float *d_
   L.rect_list = reinterpret_cast<const uint32_t *>(h->d_ws + S.o_rlist);
   L.n_rect = S.n_rect;
   L.D64 = S.o_D64 ? reinterpret_cast<double *>(h->d_ws + S.o_D64) : nullptr;
+  L.atoms8 = S.o_A8 ? reinterpret_cast<float *>(h->d_ws + S.o_A8) : nullptr;
+  L.exp_list = reinterpret_cast<const uint32_t *>(h->d_ws + S.o_elist);
+  L.n_exp = S.n_exp;
   return L;
 }
 

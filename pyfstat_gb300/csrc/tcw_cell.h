@@ -27,8 +27,10 @@
 
 #if defined(__CUDACC__)
 #define TCW_HD __host__ __device__ __forceinline__
+#define TCW_HDM __host__ __device__ __forceinline__  // member functions
 #else
 #define TCW_HD static inline
+#define TCW_HDM inline
 #include <math.h>
 #endif
 
@@ -512,7 +514,8 @@ TCW_HD float fstat_tiered2(const FF2 P[4], bool &ok) {
 // pair and C as a scalar double-word decay with r^2, (Fa_re,Fa_im) and
 // (Fb_re,Fb_im) as packed pairs with r, so each packed pair has one ratio in
 // both lanes.  Atom rows of 8 floats hold the channels in that order:
-// [a2 b2 ab 0 Fa_re Fa_im Fb_re Fb_im]; kRow8Slot[c] is the slot of channel c
+// [a2 b2 ab nz Fa_re Fa_im Fb_re Fb_im] (slot 3, nz, is an index, not a
+// channel: see ExpRow); kRow8Slot[c] is the slot of channel c
 // (a2 b2 ab Fa_re Fa_im Fb_re Fb_im).
 constexpr int kRow8Slot[7] = {0, 1, 2, 4, 5, 6, 7};
 
@@ -673,15 +676,19 @@ TCW_HD FF ff_recip(FF a) {
   return FF{s, fsub(yl, fsub(s, y))};
 }
 
-TCW_HD ExpConsts exp_consts(uint32_t TAtom, uint32_t tau) {
+// Decay constants of a window with x = TAtom / tau (tau may be real).
+TCW_HD ExpConsts exp_consts_x(double x) {
   ExpConsts k;
-  const double x = (double)TAtom / (double)tau;
   k.r1 = ff_from_double(exp(-x));
   k.r2 = ff_mul(k.r1, k.r1);
   k.has_inv = x < 60.0;
   k.r1inv = k.has_inv ? ff_recip(k.r1) : FF{0.0f, 0.0f};
   k.c1 = (float)(x * 1.4426950408889634);
   return k;
+}
+
+TCW_HD ExpConsts exp_consts(uint32_t TAtom, uint32_t tau) {
+  return exp_consts_x((double)TAtom / (double)tau);
 }
 
 TCW_HD FF ff_pow(FF r, uint32_t L) {
@@ -841,7 +848,7 @@ TCW_HD void exp_column(const float *__restrict__ atoms, const Geom &g,
 
 // ------------------------------------------------------------ packed exponential column
 // The same windows as exp_column with the atoms in 32-byte rows
-// [a2 b2 ab 0 Fa_re Fa_im Fb_re Fb_im] (one 256-bit load per step on the
+// [a2 b2 ab nz Fa_re Fa_im Fb_re Fb_im] (one 256-bit load per step on the
 // device) and the channels as three packed pairs (A,B) with r^2, (Fa) and
 // (Fb) with r, plus C as a scalar double-word with r^2: one ratio per pair,
 // so the per-column constants are two packed ratios and two packed tail
@@ -956,20 +963,17 @@ TCW_HD void exp_column2(const float *__restrict__ atoms8, const Geom &g,
         Lp = e;
         pinit = true;
         p2 = ff_mul(pw, pw);
-        ph[0] = F2{p2.h, p2.h};
-        pl[0] = F2{p2.l, p2.l};
-        ph[1] = F2{pw.h, pw.h};
-        pl[1] = F2{pw.l, pw.l};
-#pragma unroll
-        for (int c = 0; c < 2; c++) nph[c] = F2{-ph[c].x, -ph[c].y};
       }
       F2 x[4];
       TCW_DCHECK(wtop < g.numAtoms);
       load_row8(atoms8 + (size_t)wtop * 8u, x);
-      W0 = ff2_sub_scaled_x(W0, ph[0], nph[0], pl[0], x[0]);
+      // packed copies of the powers, formed here rather than held across rows
+      const F2 ph0{p2.h, p2.h}, pl0{p2.l, p2.l}, nph0{-p2.h, -p2.h};
+      const F2 ph1{pw.h, pw.h}, pl1{pw.l, pw.l}, nph1{-pw.h, -pw.h};
+      W0 = ff2_sub_scaled_x(W0, ph0, nph0, pl0, x[0]);
       Wc = ff_sub_scaled_x1(Wc, p2, x[1].x);
-      W2 = ff2_sub_scaled_x(W2, ph[1], nph[1], pl[1], x[2]);
-      W3 = ff2_sub_scaled_x(W3, ph[1], nph[1], pl[1], x[3]);
+      W2 = ff2_sub_scaled_x(W2, ph1, nph1, pl1, x[2]);
+      W3 = ff2_sub_scaled_x(W3, ph1, nph1, pl1, x[3]);
     }
     while (wlo > lo) {
       wlo--;
@@ -998,5 +1002,172 @@ TCW_HD void exp_column2(const float *__restrict__ atoms8, const Geom &g,
     sink(m, F, ok);
   }
 }
+
+
+// ------------------------------------------------------------ exponential column, row table
+// Per-row quantities of an exponential tile, tabulated once per 128 rows by
+// the warp that walks them: they depend on t0 only, so every column (lane)
+// reads the same entry (one shared-memory broadcast per cell).  The first
+// non-zero atom comes from slot 3 of the 32-byte atom rows, where the repack
+// kernel stores, for every atom i, the lowest index >= i with a2 or b2
+// non-zero.
+struct ExpRow {
+  uint32_t lo;  // exp_lo(t0): lowest atom with t_i >= t0
+  uint32_t nz;  // lowest atom >= lo with a2 or b2 non-zero (0xFFFFFFFF: none)
+  uint32_t a;   // floor((t0 - t0_data) / TAtom)
+  uint32_t b;   // (t0 - t0_data) mod TAtom
+};
+
+// Whether the window end of row t0 can use the tabulated split
+// (t0 - t0_data = a TAtom + b): t0 >= t0_data, no u32 wrap of
+// t0 + 3 tau + TAtom/2 for any tau up to taumax, and TAtom >= 2 (so the
+// quotient stays below 2^31 and the reference's cast to int keeps it).
+TCW_HD bool exp_row_regular(uint32_t t0, uint32_t taumax, const Geom &g) {
+  return g.TAtom >= 2u && t0 >= g.t0_data &&
+         (uint64_t)t0 + 3ull * (uint64_t)taumax + (uint64_t)g.half <= 0xFFFFFFFFull;
+}
+
+// One tau column: the sliding double-word window sums of exp_column2, as
+// state carried across row-table chunks.  Every arithmetic step is the same
+// as exp_column2's, in the same order, so the results are identical; only
+// the index work differs: the upper window end of a regular row is
+//     top = clamp(a + Q' + [b + R'' >= TAtom], 1, numAtoms)
+// with 3 tau + TAtom/2 = Q' TAtom + R'' fixed per column (the same
+// floor((t0 + 3 tau - t0_data + TAtom/2) / TAtom) as idx_end, without a
+// division per cell), and an empty-data window is one comparison with the
+// row's tabulated first non-zero atom.
+template <bool kFp64Det>
+struct ExpColumn {
+  ExpConsts k;
+  ExpConsts2 k2;
+  uint32_t Qp1, RmT;  // Q' + 1 and R'' - TAtom (u32 wrap)
+  FF2 W0, W2, W3;     // (A,B), (Fa_re,Fa_im), (Fb_re,Fb_im)
+  FF Wc;              // C
+  uint32_t wlo, wtop, Lp;
+  FF pw, p2;          // r^Lp and r^(2 Lp); their packed copies are formed per removal
+  bool pinit;
+
+  TCW_HDM void init(const Geom &g, uint32_t tau) {
+    k = exp_consts(g.TAtom, tau);
+    k2 = exp_consts2(k);
+    const uint32_t s = 3u * tau + g.half;  // no wrap on regular rows (checked per chunk)
+    const uint32_t Q = fdiv(s, g.div);
+    Qp1 = Q + 1u;
+    RmT = (s - Q * g.TAtom) - g.TAtom;
+    reset();
+  }
+
+  // A real tau (the differentiable statistics' continuous grid): with
+  // 3 tau + TAtom/2 = Q' TAtom + R'' (R'' real in [0, TAtom)), the carry
+  // [b + R'' >= TAtom] of an integer b is [b >= ceil(TAtom - R'')], so RmT
+  // holds -ceil(TAtom - R'') and the same top formula applies.
+  TCW_HDM void init_real(const Geom &g, double tau) {
+    k = exp_consts_x((double)g.TAtom / tau);
+    k2 = exp_consts2(k);
+    const double s = 3.0 * tau + (double)g.half;
+    const double Q = floor(s / (double)g.TAtom);
+    const double R = s - Q * (double)g.TAtom;
+    double bc = ceil((double)g.TAtom - R);
+    bc = bc < 1.0 ? 1.0 : (bc > (double)g.TAtom ? (double)g.TAtom : bc);
+    Qp1 = (uint32_t)Q + 1u;
+    RmT = 0u - (uint32_t)bc;
+    reset();
+  }
+
+  TCW_HDM void reset() {
+    const F2 z{0.0f, 0.0f};
+    W0 = W2 = W3 = FF2{z, z};
+    Wc = FF{0.0f, 0.0f};
+    wlo = wtop = 0;
+    Lp = 0;
+    pw = p2 = FF{1.0f, 0.0f};
+    pinit = false;
+  }
+
+  // Moves the window to row e's: false when it holds no atom or no data
+  // (F = 2), true when W0, Wc, W2, W3 hold its sums.
+  TCW_HDM bool window(const float *__restrict__ atoms8, const Geom &g, const ExpRow &e) {
+    const uint32_t v = e.b + RmT;  // as int: >= 0 iff b + R'' >= TAtom
+    uint32_t top = e.a + Qp1 - (v >> 31);
+    top = top < 1u ? 1u : top;
+    top = top < g.numAtoms ? top : g.numAtoms;
+    if (e.lo >= top) return false;
+    return slide(atoms8, g, e.lo, top, e.nz);
+  }
+
+  // Moves the window to the atoms [lo, top) (lo < top): false when none of
+  // them holds data (nz, the first non-zero atom >= lo, is >= top).
+  // An empty window whose next atoms enter below `top`.
+  TCW_HDM void reset_window(uint32_t top) {
+    const F2 z{0.0f, 0.0f};
+    wlo = wtop = top;
+    W0 = W2 = W3 = FF2{z, z};
+    Wc = FF{0.0f, 0.0f};
+  }
+
+  // pw = r^ex and p2 = r^(2 ex): one multiplication when the exponent moves
+  // by one, square-and-multiply otherwise.
+  TCW_HDM void power(uint32_t ex) {
+    if (ex != Lp || !pinit) {
+      if (pinit && ex == Lp + 1u)
+        pw = ff_mul(pw, k.r1);
+      else if (pinit && ex + 1u == Lp && k.has_inv)
+        pw = ff_mul(pw, ff_recip(k.r1));  // r^-1 rebuilt here: no register held for it
+      else
+        pw = ff_pow(k.r1, ex);
+      Lp = ex;
+      pinit = true;
+      p2 = ff_mul(pw, pw);
+    }
+  }
+
+  TCW_HDM bool slide(const float *__restrict__ atoms8, const Geom &g, uint32_t lo, uint32_t top,
+                     uint32_t nz) {
+    if (top > wtop || lo > wlo || top <= wlo) reset_window(top);
+    while (wtop > top) {
+      wtop--;
+      power(wtop - wlo);  // weight exponent of the leaving atom
+      F2 x[4];
+      TCW_DCHECK(wtop < g.numAtoms);
+      load_row8(atoms8 + (size_t)wtop * 8u, x);
+      // packed copies of the powers, formed here rather than held across rows
+      const F2 ph0{p2.h, p2.h}, pl0{p2.l, p2.l}, nph0{-p2.h, -p2.h};
+      const F2 ph1{pw.h, pw.h}, pl1{pw.l, pw.l}, nph1{-pw.h, -pw.h};
+      W0 = ff2_sub_scaled_x(W0, ph0, nph0, pl0, x[0]);
+      Wc = ff_sub_scaled_x1(Wc, p2, x[1].x);
+      W2 = ff2_sub_scaled_x(W2, ph1, nph1, pl1, x[2]);
+      W3 = ff2_sub_scaled_x(W3, ph1, nph1, pl1, x[3]);
+    }
+    while (wlo > lo) {
+      wlo--;
+      F2 x[4];
+      TCW_DCHECK(wlo < g.numAtoms);
+      load_row8(atoms8 + (size_t)wlo * 8u, x);
+      W0 = ff2_axpy(x[0], k2.rh[0], k2.nrh[0], k2.rl[0], W0);
+      Wc = ff_axpy(x[1].x, k.r2, Wc);
+      W2 = ff2_axpy(x[2], k2.rh[1], k2.nrh[1], k2.rl[1], W2);
+      W3 = ff2_axpy(x[3], k2.rh[1], k2.nrh[1], k2.rl[1], W3);
+    }
+    return nz < top;  // else no data in the window: zero sums, cond = inf
+  }
+
+  template <class Sink>
+  TCW_HDM void row(const float *__restrict__ atoms8, const Geom &g, const ExpRow &e, uint32_t m,
+                   Sink &sink) {
+    if (!window(atoms8, g, e)) {
+      sink(m, 2.0f, false);
+      return;
+    }
+    bool ok = true;
+    float F;
+    const F2 s0 = add2(W0.h, W0.l), s2 = add2(W2.h, W2.l), s3 = add2(W3.h, W3.l);
+    const float sc = fadd(Wc.h, Wc.l);
+    if (!fstat_fast_sums(s0.x, s0.y, sc, s2.x, s2.y, s3.x, s3.y, F)) {
+      F = fstat_ff<kFp64Det>(FF{W0.h.x, W0.l.x}, FF{W0.h.y, W0.l.y}, Wc, FF{W2.h.x, W2.l.x},
+                             FF{W2.h.y, W2.l.y}, FF{W3.h.x, W3.l.x}, FF{W3.h.y, W3.l.y}, ok);
+    }
+    sink(m, F, ok);
+  }
+};
 
 }  // namespace tcw

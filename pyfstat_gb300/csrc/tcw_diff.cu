@@ -404,6 +404,249 @@ __global__ void __launch_bounds__(kDiffBlock, diff_min_blocks(kPass))
 }
 
 
+// ------------------------------------------------------------ exponential forward (double-word)
+
+// Forward pass of exponential windows (lnBtSG and the soft-max 2F): the
+// window sums of each tau column slide down the rows in double-word FP32
+// (ExpColumn, the map kernel's arithmetic; sums good to ~1e-14 of the
+// window's magnitude, against FP64 recurrences at GB300's 1/70 FP64 rate),
+// with the per-row quantities tabulated per warp and the real tau's window
+// end split as in ExpColumn::init_real.  F goes into the FP64 log-sum-exps:
+// a cell whose FP32 tier-1 F lies more than 62 below the column's running
+// maximum carries exp(F - max) < e^-60 in both sums (the soft-max's
+// 2F/T - max is 2/T times lower still) and is skipped -- the tier-1 F is good
+// to ~1.5e-6 relative and passes only for cond < 32, where the FP64 test
+// passes too; every other cell gets F in FP64 from the double-word sums
+// (the reference's formula and conditioning test, fstat64).  Rows that are
+// not regular for the tile's taus (t0 + 3 tau + TAtom/2 beyond u32, or
+// TAtom < 2) take the window end from exp_hi_real instead.
+constexpr uint32_t kDiffRowTab = 128;
+
+__global__ void __launch_bounds__(256) diff_repack_kernel(const DiffTemplate *__restrict__ T,
+                                                          const uint32_t *__restrict__ list,
+                                                          const float *__restrict__ atoms,
+                                                          float *__restrict__ atoms8) {
+  __shared__ uint32_t s_first[256];
+  const DiffTemplate t = T[list[blockIdx.x]];
+  repack_rows256(atoms + t.atom_off * 7u, reinterpret_cast<float4 *>(atoms8 + t.atom_off * 8u),
+                 t.g.numAtoms, s_first);
+}
+
+__device__ __forceinline__ void lse_pair_add(double &m1, double &s1, double &m2, double &s2,
+                                             double F, double temp, float &skip) {
+  lse_add(m1, s1, F);
+  lse_add(m2, s2, 2.0 * F / temp);
+  skip = (float)(m1 - 62.0);
+}
+
+__global__ void __launch_bounds__(kDiffBlock, diff_min_blocks(0))
+    diff_fwd_kernel(const DiffTemplate *__restrict__ T, const DiffItem *__restrict__ items,
+                    uint32_t n_items, uint32_t *__restrict__ counter,
+                    const float *__restrict__ atoms8, const uint32_t *__restrict__ t0s_all,
+                    double temp, DiffPartial *__restrict__ parts) {
+  __shared__ uint32_t s_item;
+  __shared__ double sh[kDiffBlock / 32][4];
+  __shared__ __align__(16) ExpRow s_tab[kDiffBlock / 32][kDiffRowTab];
+  const uint32_t lane = threadIdx.x & 31u;
+  ExpRow *tab = s_tab[threadIdx.x >> 5];
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(counter, 1u);
+    __syncthreads();
+    const uint32_t it = s_item;
+    __syncthreads();
+    if (it >= n_items) break;
+    const DiffItem w = items[it];
+    const DiffTemplate t = T[w.tmpl];
+    const uint32_t n = w.n0 + threadIdx.x;
+    const bool active = n < w.n1;
+    const uint32_t *t0s = t0s_all + t.t0_off;
+    const double tau = tau_of(t, active ? n : w.n0);
+    const float *a8 = atoms8 + t.atom_off * 8u;
+    const uint32_t *a8u = reinterpret_cast<const uint32_t *>(a8);
+    double m1 = -INFINITY, s1 = 0.0, m2 = -INFINITY, s2 = 0.0;
+    float skip = -INFINITY;
+    // the warp's largest tau, rounded up, for the regularity test
+    const uint32_t tau_up = !active ? 0u
+                            : (tau >= 4294967295.0 ? 0xFFFFFFFFu : (uint32_t)ceil(tau));
+    const uint32_t taumax = __reduce_max_sync(0xffffffffu, tau_up);
+    ExpColumn<false> C;
+    C.init_real(t.g, tau);
+    for (uint32_t ce = t.N_t0; ce > 0;) {
+      const uint32_t cb = ce > kDiffRowTab ? ce - kDiffRowTab : 0u;
+      bool reg = true;
+      for (uint32_t r = lane; r < ce - cb; r += 32u)
+        reg = reg && exp_row_regular(__ldg(t0s + cb + r), taumax, t.g);
+      reg = __all_sync(0xffffffffu, reg);
+      __syncwarp();
+      for (uint32_t r = lane; r < ce - cb; r += 32u) {
+        const uint32_t t0 = __ldg(t0s + cb + r);
+        ExpRow e;
+        e.lo = exp_lo(t0, t.g);
+        e.nz = e.lo < t.g.numAtoms ? __ldg(a8u + (size_t)e.lo * 8u + 3u) : 0xFFFFFFFFu;
+        const uint32_t d = t0 - t.g.t0_data;
+        e.a = reg ? fdiv(d, t.g.div) : t0;  // irregular chunks: the generic branch reads t0
+        e.b = reg ? d - e.a * t.g.TAtom : 0u;
+        tab[r] = e;
+      }
+      __syncwarp();
+      if (active) {
+        for (uint32_t m = ce; m > cb;) {
+          m--;
+          const ExpRow e = tab[m - cb];
+          bool data;
+          if (reg) {
+            data = C.window(a8, t.g, e);
+          } else {  // the window end from the real t1 (e.a holds t0 on these rows)
+            uint32_t hi;
+            data = exp_hi_real(e.a, tau, t.g, hi) && e.lo <= hi &&
+                   C.slide(a8, t.g, e.lo, hi + 1u, e.nz);
+          }
+          double F = 2.0;
+          if (data) {
+            float F32;
+            const F2 s0 = add2(C.W0.h, C.W0.l), s2v = add2(C.W2.h, C.W2.l),
+                     s3 = add2(C.W3.h, C.W3.l);
+            const float sc = fadd(C.Wc.h, C.Wc.l);
+            if (fstat_fast_sums(s0.x, s0.y, sc, s2v.x, s2v.y, s3.x, s3.y, F32) && F32 < skip)
+              continue;
+            double W[7];
+            W[0] = (double)C.W0.h.x + (double)C.W0.l.x;
+            W[1] = (double)C.W0.h.y + (double)C.W0.l.y;
+            W[2] = (double)C.Wc.h + (double)C.Wc.l;
+            W[3] = (double)C.W2.h.x + (double)C.W2.l.x;
+            W[4] = (double)C.W2.h.y + (double)C.W2.l.y;
+            W[5] = (double)C.W3.h.x + (double)C.W3.l.x;
+            W[6] = (double)C.W3.h.y + (double)C.W3.l.y;
+            F = fstat64(W).F;
+          } else if (2.0f < skip) {
+            continue;
+          }
+          lse_pair_add(m1, s1, m2, s2, F, temp, skip);
+        }
+      }
+      ce = cb;
+    }
+    // block merge of the two log-sum-exp pairs (warp shuffles, then smem)
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+      const double om1 = __shfl_down_sync(0xffffffffu, m1, d);
+      const double os1 = __shfl_down_sync(0xffffffffu, s1, d);
+      const double om2 = __shfl_down_sync(0xffffffffu, m2, d);
+      const double os2 = __shfl_down_sync(0xffffffffu, s2, d);
+      lse_merge(m1, s1, om1, os1);
+      lse_merge(m2, s2, om2, os2);
+    }
+    if (lane == 0) {
+      sh[threadIdx.x >> 5][0] = m1;
+      sh[threadIdx.x >> 5][1] = s1;
+      sh[threadIdx.x >> 5][2] = m2;
+      sh[threadIdx.x >> 5][3] = s2;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int k = 1; k < kDiffBlock / 32; k++) {
+        lse_merge(m1, s1, sh[k][0], sh[k][1]);
+        lse_merge(m2, s2, sh[k][2], sh[k][3]);
+      }
+      parts[w.part] = DiffPartial{m1, s1, m2, s2};
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------ exponential backward (double-word)
+
+// Packed double-word helpers of the backward pass.
+__device__ __forceinline__ FF2 ff2_add_dw(FF2 a, FF2 b) {  // a + b, low words summed
+  const F2 s = add2(a.h, b.h);
+  const F2 bb = sub2(s, a.h);
+  const F2 e = add2(sub2(a.h, sub2(s, bb)), sub2(b.h, bb));
+  return FF2{s, add2(e, add2(a.l, b.l))};
+}
+__device__ __forceinline__ FF2 ff2_scale_dw(F2 rh, F2 nrh, F2 rl, FF2 S) {  // r S (r = rh + rl)
+  const F2 q = mul2(nrh, S.h);  // -p
+  F2 pe = fma2(rh, S.h, q);
+  pe = fma2(rh, S.l, pe);
+  pe = fma2(rl, S.h, pe);
+  return FF2{sub2(F2{0.0f, 0.0f}, q), pe};
+}
+__device__ __forceinline__ FF ff_add_dw(FF a, FF b) {
+  float s, e;
+  two_sum(a.h, b.h, s, e);
+  return FF{s, fadd(e, fadd(a.l, b.l))};
+}
+__device__ __forceinline__ FF ff_scale_dw(FF r, FF S) {
+  const float p = fmul(r.h, S.h);
+  float pe = ffma(r.h, S.h, -p);
+  pe = ffma(r.h, S.l, pe);
+  pe = ffma(r.l, S.h, pe);
+  return FF{p, pe};
+}
+__device__ __forceinline__ double dw_value(float h, float l) { return (double)h + (double)l; }
+
+// The backward pass's column: the window sums W of ExpColumn and their
+// tau-derivative sums V_c = sum_i (i - lo) x_c(i) r_c^(i - lo) (r_c = r^2
+// for A, B, C, r for Fa, Fb), both in double-word FP32 and moved together:
+// an atom entering at the bottom gives V' = r_c (V + W) (the old W), one
+// leaving at the top with weight exponent e gives V' = V - e x r_c^e.
+// dW_c / dtau = k_c (TAtom / tau^2) V_c (k_c = 2 for A, B, C; 1 otherwise).
+struct ExpColumnV {
+  ExpColumn<false> C;
+  FF2 V0, V2, V3;
+  FF Vc;
+
+  __device__ __forceinline__ void reset_v() {
+    const F2 z{0.0f, 0.0f};
+    V0 = V2 = V3 = FF2{z, z};
+    Vc = FF{0.0f, 0.0f};
+  }
+
+  __device__ __forceinline__ bool slide(const float *__restrict__ atoms8, const Geom &g,
+                                        uint32_t lo, uint32_t top, uint32_t nz) {
+    if (top > C.wtop || lo > C.wlo || top <= C.wlo) {
+      C.reset_window(top);
+      reset_v();
+    }
+    while (C.wtop > top) {
+      C.wtop--;
+      const uint32_t ex = C.wtop - C.wlo;
+      C.power(ex);
+      F2 x[4];
+      TCW_DCHECK(C.wtop < g.numAtoms);
+      load_row8(atoms8 + (size_t)C.wtop * 8u, x);
+      const F2 ph0{C.p2.h, C.p2.h}, pl0{C.p2.l, C.p2.l}, nph0{-C.p2.h, -C.p2.h};
+      const F2 ph1{C.pw.h, C.pw.h}, pl1{C.pw.l, C.pw.l}, nph1{-C.pw.h, -C.pw.h};
+      C.W0 = ff2_sub_scaled_x(C.W0, ph0, nph0, pl0, x[0]);
+      C.Wc = ff_sub_scaled_x1(C.Wc, C.p2, x[1].x);
+      C.W2 = ff2_sub_scaled_x(C.W2, ph1, nph1, pl1, x[2]);
+      C.W3 = ff2_sub_scaled_x(C.W3, ph1, nph1, pl1, x[3]);
+      // V: the leaving atom's weight times its exponent
+      const FF e2 = ff_mul(C.p2, FF{(float)ex, 0.0f}), e1 = ff_mul(C.pw, FF{(float)ex, 0.0f});
+      const F2 eh0{e2.h, e2.h}, el0{e2.l, e2.l}, neh0{-e2.h, -e2.h};
+      const F2 eh1{e1.h, e1.h}, el1{e1.l, e1.l}, neh1{-e1.h, -e1.h};
+      V0 = ff2_sub_scaled_x(V0, eh0, neh0, el0, x[0]);
+      Vc = ff_sub_scaled_x1(Vc, e2, x[1].x);
+      V2 = ff2_sub_scaled_x(V2, eh1, neh1, el1, x[2]);
+      V3 = ff2_sub_scaled_x(V3, eh1, neh1, el1, x[3]);
+    }
+    while (C.wlo > lo) {
+      C.wlo--;
+      F2 x[4];
+      TCW_DCHECK(C.wlo < g.numAtoms);
+      load_row8(atoms8 + (size_t)C.wlo * 8u, x);
+      V0 = ff2_scale_dw(C.k2.rh[0], C.k2.nrh[0], C.k2.rl[0], ff2_add_dw(V0, C.W0));
+      Vc = ff_scale_dw(C.k.r2, ff_add_dw(Vc, C.Wc));
+      V2 = ff2_scale_dw(C.k2.rh[1], C.k2.nrh[1], C.k2.rl[1], ff2_add_dw(V2, C.W2));
+      V3 = ff2_scale_dw(C.k2.rh[1], C.k2.nrh[1], C.k2.rl[1], ff2_add_dw(V3, C.W3));
+      C.W0 = ff2_axpy(x[0], C.k2.rh[0], C.k2.nrh[0], C.k2.rl[0], C.W0);
+      C.Wc = ff_axpy(x[1].x, C.k.r2, C.Wc);
+      C.W2 = ff2_axpy(x[2], C.k2.rh[1], C.k2.nrh[1], C.k2.rl[1], C.W2);
+      C.W3 = ff2_axpy(x[3], C.k2.rh[1], C.k2.nrh[1], C.k2.rl[1], C.W3);
+    }
+    return nz < top;
+  }
+};
+
 // ------------------------------------------------------------ rectangular windows
 
 // Inclusive end index of a rectangular window for a real tau (the
@@ -600,7 +843,7 @@ __global__ void diff_finalize_kernel(const DiffTemplate *__restrict__ T, uint32_
 int diff_blocks_per_sm(int pass) {
   int n = 0;
   cudaError_t e = pass == 0
-                      ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, diff_kernel<0>, kDiffBlock, 0)
+                      ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, diff_fwd_kernel, kDiffBlock, 0)
                       : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, diff_kernel<1>, kDiffBlock, 0);
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -624,11 +867,11 @@ int rect_diff_blocks_per_sm(int pass) {
 
 cudaError_t launch_diff(int pass, const DiffLaunch &L, cudaStream_t stream) {
   if (L.n_items) {
-    if (pass == 0)
-      diff_kernel<0><<<L.n_blocks, kDiffBlock, 0, stream>>>(
-          L.T, L.items, L.n_items, L.counter, L.atoms, L.t0s, L.temp, L.parts, nullptr, nullptr,
-          nullptr, nullptr, nullptr, 0, nullptr, nullptr);
-    else
+    if (pass == 0) {
+      diff_repack_kernel<<<L.n_exp, 256, 0, stream>>>(L.T, L.exp_list, L.atoms, L.atoms8);
+      diff_fwd_kernel<<<L.n_blocks, kDiffBlock, 0, stream>>>(L.T, L.items, L.n_items, L.counter,
+                                                             L.atoms8, L.t0s, L.temp, L.parts);
+    } else
       diff_kernel<1><<<L.n_blocks, kDiffBlock, 0, stream>>>(
           L.T, L.items, L.n_items, L.counter, L.atoms, L.t0s, L.temp, nullptr, L.lnZ1, L.lnZ2,
           L.gB, L.gS, L.scratch, L.scratch_rows, L.grad_atoms, L.grad_tau);

@@ -57,6 +57,46 @@ struct Partial {
   double s;
 };
 
+#if defined(__CUDACC__)
+// One template's atoms (rows of 7 floats, x) into 32-byte rows
+// [a2 b2 ab nz Fa_re Fa_im Fb_re Fb_im] (o), by one block of 256 threads;
+// nz (as u32 bits) is the lowest atom index >= i with a2 or b2 non-zero
+// (0xFFFFFFFF: none).  Each thread owns a contiguous chunk of atoms and walks
+// it backwards, starting from the first non-zero atom of the chunks above it.
+__device__ __forceinline__ void repack_rows256(const float *__restrict__ x,
+                                               float4 *__restrict__ o, uint32_t N,
+                                               uint32_t *s_first) {
+  const uint32_t tid = threadIdx.x;
+  const uint32_t chunk = (N + 255u) / 256u;
+  const uint32_t i0 = min(N, tid * chunk), i1 = min(N, i0 + chunk);
+  uint32_t first = 0xFFFFFFFFu;
+  for (uint32_t i = i0; i < i1; i++) {
+    const float *r = x + (size_t)i * 7u;
+    if (__ldg(r) != 0.0f || __ldg(r + 1) != 0.0f) {
+      first = i;
+      break;
+    }
+  }
+  s_first[tid] = first;
+  __syncthreads();
+  uint32_t nz = 0xFFFFFFFFu;
+  for (uint32_t k = tid + 1u; k < 256u; k++) {
+    if (s_first[k] != 0xFFFFFFFFu) {
+      nz = s_first[k];
+      break;
+    }
+  }
+  for (uint32_t i = i1; i > i0;) {
+    i--;
+    const float *r = x + (size_t)i * 7u;
+    const float a2 = __ldg(r), b2 = __ldg(r + 1);
+    if (a2 != 0.0f || b2 != 0.0f) nz = i;
+    o[2u * i] = make_float4(a2, b2, __ldg(r + 2), __uint_as_float(nz));
+    o[2u * i + 1u] = make_float4(__ldg(r + 3), __ldg(r + 4), __ldg(r + 5), __ldg(r + 6));
+  }
+}
+#endif
+
 // Launchers (tcw_kernels.cu).  All asynchronous on `stream`.
 cudaError_t launch_prefix(const TemplateDev *d_T, const uint32_t *d_rect_list, uint32_t n_rect,
                           const float *d_atoms, float *d_P, int prec, cudaStream_t stream);
@@ -119,6 +159,10 @@ struct DiffLaunch {
   uint32_t n_items, n_blocks;
   uint32_t *counter;
   const float *atoms;
+  float *atoms8;                     // pass A: exponential templates' atoms in 32-byte rows
+                                     // (same row index as `atoms`), written by the launch
+  const uint32_t *exp_list;          // pass A: the exponential templates' indices
+  uint32_t n_exp;
   const uint32_t *t0s;
   double temp;
   DiffPartial *parts;                // pass A output

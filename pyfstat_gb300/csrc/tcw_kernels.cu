@@ -62,15 +62,10 @@ __global__ void __launch_bounds__(256) repack_kernel(const TemplateDev *__restri
                                                      const uint32_t *__restrict__ exp_list,
                                                      const float *__restrict__ atoms,
                                                      float *__restrict__ A8) {
+  __shared__ uint32_t s_first[256];
   const TemplateDev t = T[exp_list[blockIdx.x]];
-  const float *x = atoms + t.atom_off * 7u;
-  float4 *o = reinterpret_cast<float4 *>(A8 + t.a8_off * 8u);
-  for (uint32_t i = threadIdx.x; i < t.g.numAtoms; i += blockDim.x) {
-    const float *r = x + (size_t)i * 7u;
-    // row layout kRow8Slot: [a2 b2 ab 0 Fa_re Fa_im Fb_re Fb_im]
-    o[2u * i] = make_float4(__ldg(r), __ldg(r + 1), __ldg(r + 2), 0.0f);
-    o[2u * i + 1u] = make_float4(__ldg(r + 3), __ldg(r + 4), __ldg(r + 5), __ldg(r + 6));
-  }
+  repack_rows256(atoms + t.atom_off * 7u, reinterpret_cast<float4 *>(A8 + t.a8_off * 8u),
+                 t.g.numAtoms, s_first);
 }
 
 // ------------------------------------------------------------------ prefix
@@ -420,43 +415,81 @@ struct MapSink {
   }
 };
 
-// Exponential tile: each thread runs one tau column over a chunk of rows.
-// The lower window end depends on t0 only and is tabulated once per tile in
-// shared memory (lo_tab, kExpLoTab entries; longer tiles compute it inline).
-constexpr uint32_t kExpLoTab = 2048;
+// Exponential tile: each thread runs one tau column over a chunk of rows
+// (the chunk is the same for the 32 lanes of a warp: tn >= 32).  When every
+// row of the warp's chunk satisfies exp_row_regular for its columns' largest
+// tau, the per-row quantities (ExpRow: window start, first non-zero atom,
+// t0 split by TAtom) are tabulated 128 rows at a time by the warp itself in
+// its own shared-memory slots (no block barrier) and every cell takes the
+// division-free window end of ExpColumn; otherwise the warp runs
+// exp_column2's generic index arithmetic.  Both give identical results.
+constexpr uint32_t kExpRowTab = 128;
 
 template <bool kWrite, int kPrec>
 __device__ void exp_tile(const TemplateDev &t, const WorkItem &w, const float *__restrict__ atoms,
                          const float *__restrict__ atoms8,
                          const uint32_t *__restrict__ t0s_all,
                          const uint32_t *__restrict__ taus_all, float *__restrict__ Fmn,
-                         Red &red, uint32_t *lo_tab) {
+                         Red &red, ExpRow *tab, bool warp_tile = false) {
   const uint32_t *t0s = t0s_all + t.t0_off;
-  const uint32_t rows = w.m1 - w.m0;
-  const bool use_tab = rows <= kExpLoTab;
-  if (use_tab) {
-    for (uint32_t r = threadIdx.x; r < rows; r += blockDim.x)
-      lo_tab[r] = exp_lo(__ldg(t0s + w.m0 + r), t.g);
-  }
-  __syncthreads();
   const uint32_t tn = w.tn;
-  const uint32_t col = threadIdx.x % tn, rl = threadIdx.x / tn;
+  const uint32_t lane = threadIdx.x & 31u;
+  // a warp tile (persistent launches) is 32 columns over all the tile's rows
+  const uint32_t col = warp_tile ? lane : threadIdx.x % tn;
+  const uint32_t rl = warp_tile ? 0u : threadIdx.x / tn;
   const uint32_t n = w.n0 + col;
   const uint32_t R = w.rows_per_lane;
   const uint32_t mb = w.m0 + rl * R;
-  if (n < w.n1 && mb < w.m1) {
-    const uint32_t me = min(w.m1, mb + R);
-    const uint32_t tau = __ldg(taus_all + t.tau_off + n);
-    MapSink<kWrite> sink{kWrite ? Fmn + t.map_off : nullptr, t.N_tau, n, &red};
-    const uint32_t *tab = use_tab ? lo_tab + (mb - w.m0) : nullptr;
-    if (kPrec == kPrecPlain32)
-      exp_column<false, false>(atoms + t.atom_off * 7u, t.g, t0s, mb, me, tau, sink, tab);
-    else if (kPrec == kPrecFF_F64Det)
-      exp_column2<true>(atoms8 + t.a8_off * 8u, t.g, t0s, mb, me, tau, sink, tab);
-    else
-      exp_column2<false>(atoms8 + t.a8_off * 8u, t.g, t0s, mb, me, tau, sink, tab);
-    red.row_to_index(t.N_tau, n);
+  if (mb >= w.m1) return;  // uniform per warp (tn >= 32)
+  const uint32_t me = min(w.m1, mb + R);
+  const bool active = n < w.n1;
+  const uint32_t tau = active ? __ldg(taus_all + t.tau_off + n) : 0u;
+  MapSink<kWrite> sink{kWrite ? Fmn + t.map_off : nullptr, t.N_tau, n, &red};
+  if (kPrec == kPrecPlain32) {
+    if (active) {
+      exp_column<false, false>(atoms + t.atom_off * 7u, t.g, t0s, mb, me, tau, sink, nullptr);
+      red.row_to_index(t.N_tau, n);
+    }
+    return;
   }
+  const float *a8 = atoms8 + t.a8_off * 8u;
+  const uint32_t taumax = __reduce_max_sync(0xffffffffu, tau);
+  bool reg = true;
+  for (uint32_t m = mb + lane; m < me; m += 32u)
+    reg = reg && exp_row_regular(__ldg(t0s + m), taumax, t.g);
+  if (!__all_sync(0xffffffffu, reg)) {
+    if (active) {
+      exp_column2<kPrec == kPrecFF_F64Det>(a8, t.g, t0s, mb, me, tau, sink, nullptr);
+      red.row_to_index(t.N_tau, n);
+    }
+    return;
+  }
+  const uint32_t *a8u = reinterpret_cast<const uint32_t *>(a8);
+  ExpColumn<kPrec == kPrecFF_F64Det> C;
+  C.init(t.g, tau);
+  for (uint32_t ce = me; ce > mb;) {
+    const uint32_t cb = ce - mb > kExpRowTab ? ce - kExpRowTab : mb;
+    __syncwarp();
+    for (uint32_t r = lane; r < ce - cb; r += 32u) {
+      const uint32_t t0 = __ldg(t0s + cb + r);
+      ExpRow e;
+      e.lo = exp_lo(t0, t.g);
+      e.nz = e.lo < t.g.numAtoms ? __ldg(a8u + (size_t)e.lo * 8u + 3u) : 0xFFFFFFFFu;
+      const uint32_t d = t0 - t.g.t0_data;
+      e.a = fdiv(d, t.g.div);
+      e.b = d - e.a * t.g.TAtom;
+      tab[r] = e;
+    }
+    __syncwarp();
+    if (active) {
+      for (uint32_t m = ce; m > cb;) {
+        m--;
+        C.row(a8, t.g, tab[m - cb], m, sink);
+      }
+    }
+    ce = cb;
+  }
+  if (active) red.row_to_index(t.N_tau, n);
 }
 
 // Minimum resident blocks per SM requested from the register allocator
@@ -493,7 +526,7 @@ __global__ void __launch_bounds__(kBlock, (map_min_blocks<kWin, kPersist, kWrite
                Partial *__restrict__ parts) {
   __shared__ uint32_t s_item;
   constexpr uint32_t kSmem = kWin == TCW_WINDOW_RECT ? (kWrite ? (kBlock / 32) * 32 * 33 : 1)
-                                                     : kExpLoTab;
+                                                     : (kBlock / 32) * kExpRowTab * 4;
   __shared__ __align__(16) uint32_t sm[kSmem];
   __shared__ uint32_t s_tau[kWin == TCW_WINDOW_RECT ? kBlock : 1];
   if (kWin == TCW_WINDOW_RECT && kPersist) {
@@ -531,6 +564,38 @@ __global__ void __launch_bounds__(kBlock, (map_min_blocks<kWin, kPersist, kWrite
     }
     return;
   }
+  if (kWin == TCW_WINDOW_EXP && kPersist) {
+    // Persistent exponential launches schedule by warp as well: each warp
+    // fetches 32-column tiles (all rows of a row chunk), keeps its row table
+    // in its own shared-memory slots and reduces its tile itself, so no block
+    // barrier waits for the warp with the most removals.
+    const uint32_t lane = threadIdx.x & 31u;
+    ExpRow *tab = reinterpret_cast<ExpRow *>(sm) + (threadIdx.x >> 5) * kExpRowTab;
+    for (;;) {
+      uint32_t it2 = 0;
+      if (lane == 0) it2 = atomicAdd(counter, 1u);
+      it2 = __shfl_sync(0xffffffffu, it2, 0);
+      if (it2 >= n_items) break;
+      const WorkItem w = items[it2];
+      const TemplateDev t = T[w.tmpl];
+      Red red;
+      red.init();
+      exp_tile<kWrite, kPrec>(t, w, atoms, atoms8, t0s, taus, Fmn, red, tab, true);
+      RedVal acc{red.mx, red.bidx, fsub(red.s, red.c)};
+#pragma unroll
+      for (int d = 16; d > 0; d >>= 1) acc = red_combine(acc, shfl_down_red(acc, d));
+      if (lane == 0) {
+        Partial pp;
+        pp.maxF = acc.mx;
+        pp.pad = 0;
+        pp.argmax = acc.bidx;
+        pp.s = (acc.mx == -INFINITY) ? 0.0 : (double)acc.s;
+        parts[w.part] = pp;
+      }
+      __syncwarp();
+    }
+    return;
+  }
   uint32_t it = blockIdx.x;
   for (;;) {
     if (kPersist) {
@@ -550,7 +615,8 @@ __global__ void __launch_bounds__(kBlock, (map_min_blocks<kWin, kPersist, kWrite
                                reinterpret_cast<float *>(sm) + warp * (32 * 33), warp % rg,
                                4u / rg, warp / rg, s_tau + warp * 32u);
     } else
-      exp_tile<kWrite, kPrec>(t, w, atoms, atoms8, t0s, taus, Fmn, red, sm);
+      exp_tile<kWrite, kPrec>(t, w, atoms, atoms8, t0s, taus, Fmn, red,
+                              reinterpret_cast<ExpRow *>(sm) + (threadIdx.x >> 5) * kExpRowTab);
     block_reduce_store(red, parts + w.part);
     if (!kPersist) break;
   }

@@ -83,7 +83,11 @@ struct HostSink {
   }
 };
 
-// comp = 1: the packed column the GPU runs (atoms in rows of 8);
+// comp = 1: what the GPU runs -- atoms in rows of 8 with the first-non-zero
+//           index in slot 3 (as the repack kernel writes them), each row
+//           chunk through the row-table column (ExpColumn) when all its rows
+//           are regular for the column's tau, else through exp_column2;
+// comp = 2: exp_column2 only (the generic index arithmetic);
 // comp = 0: the uncompensated FP32 variant.
 int hc_exp_map(const float *atoms, uint32_t n, uint32_t TAtom, uint32_t t0_data,
                const uint32_t *t0s, uint32_t N_t0, const uint32_t *taus, uint32_t N_tau,
@@ -92,16 +96,79 @@ int hc_exp_map(const float *atoms, uint32_t n, uint32_t TAtom, uint32_t t0_data,
   if (row_chunk == 0) row_chunk = N_t0;
   float *a8 = (float *)calloc((size_t)n * 8u, sizeof(float));
   if (!a8) return -1;
-  for (uint32_t i = 0; i < n; i++)
+  uint32_t nz = 0xFFFFFFFFu;
+  for (uint32_t i = n; i-- > 0;) {
     for (int c = 0; c < 7; c++) a8[(size_t)i * 8u + kRow8Slot[c]] = atoms[(size_t)i * 7u + c];
+    if (atoms[(size_t)i * 7u] != 0.0f || atoms[(size_t)i * 7u + 1u] != 0.0f) nz = i;
+    memcpy(&a8[(size_t)i * 8u + 3u], &nz, sizeof(nz));
+  }
   for (uint32_t k = 0; k < N_tau; k++) {
     for (uint32_t mb = 0; mb < N_t0; mb += row_chunk) {
       uint32_t me = mb + row_chunk < N_t0 ? mb + row_chunk : N_t0;
       HostSink s{F + k, okmap ? okmap + k : nullptr, N_tau};
-      if (comp)
+      bool reg = comp == 1;
+      for (uint32_t m = mb; reg && m < me; m++) reg = exp_row_regular(t0s[m], taus[k], g);
+      if (reg) {
+        ExpColumn<false> C;
+        C.init(g, taus[k]);
+        for (uint32_t m = me; m-- > mb;) {
+          ExpRow e;
+          e.lo = exp_lo(t0s[m], g);
+          e.nz = 0xFFFFFFFFu;
+          if (e.lo < n) memcpy(&e.nz, &a8[(size_t)e.lo * 8u + 3u], sizeof(e.nz));
+          const uint32_t d = t0s[m] - t0_data;
+          e.a = fdiv(d, g.div);
+          e.b = d - e.a * TAtom;
+          C.row(a8, g, e, m, s);
+        }
+      } else if (comp) {
         exp_column2<false>(a8, g, t0s, mb, me, taus[k], s);
-      else
+      } else {
         exp_column<false, false>(atoms, g, t0s, mb, me, taus[k], s);
+      }
+    }
+  }
+  free(a8);
+  return 0;
+}
+
+// Window sums of exponential windows on a real tau grid (the differentiable
+// statistics' forward pass): the double-word sums of ExpColumn (init_real,
+// row tables) as FP64 values, W[(m * N_tau + n) * 7 + c], and whether the
+// window holds data.  Rows must be regular for every tau (t0 >= t0_data).
+int hc_exp_real_sums(const float *atoms, uint32_t n, uint32_t TAtom, uint32_t t0_data,
+                     const uint32_t *t0s, uint32_t N_t0, const double *taus, uint32_t N_tau,
+                     double *W, uint8_t *valid) {
+  Geom g = make_geom(n, TAtom, t0_data);
+  float *a8 = (float *)calloc((size_t)n * 8u, sizeof(float));
+  if (!a8) return -1;
+  uint32_t nz = 0xFFFFFFFFu;
+  for (uint32_t i = n; i-- > 0;) {
+    for (int c = 0; c < 7; c++) a8[(size_t)i * 8u + kRow8Slot[c]] = atoms[(size_t)i * 7u + c];
+    if (atoms[(size_t)i * 7u] != 0.0f || atoms[(size_t)i * 7u + 1u] != 0.0f) nz = i;
+    memcpy(&a8[(size_t)i * 8u + 3u], &nz, sizeof(nz));
+  }
+  for (uint32_t k = 0; k < N_tau; k++) {
+    ExpColumn<false> C;
+    C.init_real(g, taus[k]);
+    for (uint32_t m = N_t0; m-- > 0;) {
+      ExpRow e;
+      e.lo = exp_lo(t0s[m], g);
+      e.nz = 0xFFFFFFFFu;
+      if (e.lo < n) memcpy(&e.nz, &a8[(size_t)e.lo * 8u + 3u], sizeof(e.nz));
+      const uint32_t d = t0s[m] - t0_data;
+      e.a = fdiv(d, g.div);
+      e.b = d - e.a * TAtom;
+      const bool ok = C.window(a8, g, e);
+      double *w = W + ((size_t)m * N_tau + k) * 7u;
+      w[0] = (double)C.W0.h.x + (double)C.W0.l.x;
+      w[1] = (double)C.W0.h.y + (double)C.W0.l.y;
+      w[2] = (double)C.Wc.h + (double)C.Wc.l;
+      w[3] = (double)C.W2.h.x + (double)C.W2.l.x;
+      w[4] = (double)C.W2.h.y + (double)C.W2.l.y;
+      w[5] = (double)C.W3.h.x + (double)C.W3.l.x;
+      w[6] = (double)C.W3.h.y + (double)C.W3.l.y;
+      valid[(size_t)m * N_tau + k] = ok;
     }
   }
   free(a8);

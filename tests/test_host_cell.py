@@ -147,3 +147,96 @@ def test_exp_long_columns_many_removals(hostcell, oracle, dt0):
     F, _ = hc_map(hostcell, c)
     rel, _ = rel_err(F, F64, cond)
     assert rel.max() < REL_TOL, rel.max()
+
+
+def test_exp_row_table_column_equals_generic_column(hostcell):
+    """The row-table column (tabulated window starts and first non-zero atoms,
+    division-free window ends; what the GPU runs on regular rows) gives
+    bit-identical maps to the generic column on the same row chunks: random
+    grids (regular ones and ones starting before the data, which fall back to
+    the generic arithmetic), TAtom other than 1800, non-uniform t0 grids."""
+    from _helpers import P
+
+    checked = 0
+    for seed in range(30):
+        rng = np.random.default_rng(500 + seed)
+        TAtom = 1800 if seed % 3 else int(rng.integers(2, 5000))
+        t0_data, A = synth.merged_atoms(seed, int(rng.integers(5, 250)), int(rng.integers(1, 3)),
+                                        Tsft=TAtom, gap_frac=float(rng.uniform(0, 0.4)))
+        A = A.copy()
+        for _ in range(int(rng.integers(0, 3))):
+            s = int(rng.integers(0, A.shape[0]))
+            A[s:s + int(rng.integers(1, 30))] = 0
+        nt0, ntau = int(rng.integers(1, 150)), int(rng.integers(1, 60))
+        if seed % 4 == 0:  # non-uniform, sorted t0 grid inside the data
+            t0s = np.sort(rng.integers(t0_data, t0_data + A.shape[0] * TAtom, nt0))
+        else:
+            t0 = int(t0_data + rng.integers(-3 * TAtom if seed % 5 == 0 else 0, 2 * TAtom))
+            t0s = t0 + np.arange(nt0) * int(rng.integers(1, 3 * TAtom))
+        t0s = t0s.astype(np.uint32)
+        taus = (int(rng.integers(1, 4 * TAtom)) + np.arange(ntau) *
+                int(rng.integers(0, 5 * TAtom))).astype(np.uint32)
+        row_chunk = int(rng.integers(0, 40))
+        out = []
+        for comp in (1, 2):
+            F = np.empty((nt0, ntau), np.float32)
+            hostcell.hc_exp_map(A.ctypes.data_as(P), ctypes.c_uint32(A.shape[0]),
+                                ctypes.c_uint32(TAtom), ctypes.c_uint32(t0_data),
+                                t0s.ctypes.data_as(P), ctypes.c_uint32(nt0),
+                                taus.ctypes.data_as(P), ctypes.c_uint32(ntau), ctypes.c_int(comp),
+                                ctypes.c_uint32(row_chunk), F.ctypes.data_as(P),
+                                None)
+            out.append(F)
+        assert np.array_equal(out[0].view(np.uint32), out[1].view(np.uint32)), seed
+        checked += out[0].size
+    assert checked > 50000
+
+
+def test_exp_real_tau_window_sums_match_fp64(hostcell):
+    """The forward pass of the differentiable statistics: double-word window
+    sums on a real tau grid (window ends from the split 3 tau + TAtom/2 =
+    Q' TAtom + R'', R'' real) against FP64 sums over the reference's window
+    (t0 <= t_i <= t0 + 3 tau, i <= floor((t0 + 3 tau - t0_data + TAtom/2) /
+    TAtom) - 1; the FP64 torch reference's mask), on grids with real taus
+    and, for every data window, relative to the sum of |terms|."""
+    import _torch_ref as R
+    from _helpers import P
+
+    for seed in range(6):
+        rng = np.random.default_rng(900 + seed)
+        t0_data, A = synth.merged_atoms(seed, int(rng.integers(20, 160)), 2,
+                                        gap_frac=float(rng.uniform(0, 0.3)))
+        nt0, ntau = int(rng.integers(3, 40)), int(rng.integers(2, 30))
+        t0s = (t0_data + int(rng.integers(0, 900)) +
+               np.arange(nt0) * int(rng.integers(300, 4000))).astype(np.uint32)
+        tau_min = float(rng.uniform(500, 5000))
+        taus = tau_min + np.arange(ntau) * float(rng.uniform(10, 3000))
+        W = np.empty((nt0, ntau, 7), np.float64)
+        ok = np.empty((nt0, ntau), np.uint8)
+        assert hostcell.hc_exp_real_sums(
+            A.ctypes.data_as(P), ctypes.c_uint32(A.shape[0]), ctypes.c_uint32(1800),
+            ctypes.c_uint32(t0_data), t0s.ctypes.data_as(P), ctypes.c_uint32(nt0),
+            taus.ctypes.data_as(P), ctypes.c_uint32(ntau), W.ctypes.data_as(P),
+            ok.ctypes.data_as(P)) == 0
+        mask = R.window_mask(A.shape[0], 1800, t0_data, t0s, taus, window=2)
+        t_i = t0_data + np.arange(A.shape[0]) * 1800.0
+        dt = np.clip(t_i[None, None, :] - t0s.astype(np.float64)[:, None, None], 0, None)
+        w = np.where(mask, np.exp(-dt / taus[None, :, None]), 0.0)
+        for c in range(7):
+            wk = w * w if c < 3 else w
+            # the double-word sums leave out the window's common factor
+            # e^(-k (t_lo - t0) / tau): compare after scaling to the first atom
+            ref = np.einsum("mni,i->mn", wk, A[:, c].astype(np.float64))
+            absref = np.einsum("mni,i->mn", wk, np.abs(A[:, c]).astype(np.float64))
+            lo = np.argmax(mask, axis=2)
+            t_lo = t0_data + lo * 1800.0
+            k = 2.0 if c < 3 else 1.0
+            scale = np.exp(-k * (t_lo - t0s.astype(np.float64)[:, None]) / taus[None, :])
+            has = mask.any(axis=2) & (ok == 1)
+            got = W[:, :, c] * scale
+            err = np.abs(got - ref)[has] / np.maximum(absref[has], 1e-300)
+            assert err.size == 0 or err.max() < 1e-11, (seed, c, err.max())
+        # a window without data in the reference mask (or only zero atoms) is not valid
+        nodata = ~(mask & ((A[:, 0] != 0) | (A[:, 1] != 0))[None, None, :]).any(axis=2)
+        assert np.all(ok[nodata] == 0), seed
+        assert np.all(ok[~nodata] == 1), seed
