@@ -54,12 +54,15 @@ def parse():
                    help="templates timed with the plain per-template kernel")
     p.add_argument("--window", choices=["both", "rect", "exp"], default="both",
                    help="restrict the workload to one window type (breakdown runs)")
-    p.add_argument("--case", choices=["plain-rect", "plain-exp", "single-480"], default=None,
+    p.add_argument("--case", choices=["plain-rect", "plain-exp", "single-480", "grad"],
+                   default=None,
                    help="instead of the benchmark: time one single-template map with the map "
                         "written (8192 t0 x 4096 tau over one year of two-detector data; the "
                         "134 MB map exceeds L2), for the memory-side profile of the plain kernel; "
                         "single-480: the 480 x 480 rect and 480 x 512 log-tau exp single-template "
-                        "maps on device buffers (--steps calls each)")
+                        "maps on device buffers (--steps calls each); grad: the differentiation "
+                        "workload alone (the first --templates of its 256 templates, --steps "
+                        "repetitions)")
     p.add_argument("--tile", type=str, default="auto",
                    help="tile config as JSON, 'auto' for the autotuner (default), "
                         "'default' for the library defaults")
@@ -307,7 +310,7 @@ def plain_configs(h, dev, torch, stream, hbm, reps=200):
 GRAD_FP64_FLOPS = {"forward": 55.0, "backward": 110.0}
 
 
-def grad_case(torch, dev, peaks, reps=3):
+def grad_case(torch, dev, peaks, reps=3, n_templates=256):
     """Differentiation workload: 256 templates x 2000 SFTs x 2 detectors,
     exponential windows, 1024 t0 x 1024 tau; forward (lnBtSG and soft-max 2F)
     and backward (gradients of both w.r.t. atoms and tau), CUDA events."""
@@ -315,7 +318,7 @@ def grad_case(torch, dev, peaks, reps=3):
     from pyfstat_gb300.autograd import DiffBatch
 
     tl = []
-    for k in range(256):
+    for k in range(n_templates):
         t0_data, A = synth.merged_atoms(5000 + k, 2000, 2)
         tl.append(dict(atoms=A, TAtom=1800, t0_data=t0_data, t0=t0_data + 450, dt0=3600,
                        N_t0=1024, N_tau=1024, tau_min=30075.0,
@@ -324,7 +327,7 @@ def grad_case(torch, dev, peaks, reps=3):
     atoms = torch.from_numpy(b.atoms).to(dev)
     tmin = np.array([t["tau_min"] for t in tl])
     tmax = np.array([t["tau_max"] for t in tl])
-    one = torch.ones(256, dtype=torch.float64, device=dev)
+    one = torch.ones(n_templates, dtype=torch.float64, device=dev)
     lnB, soft = b.forward_raw(atoms, tmin, tmax)
     b.backward_raw(atoms, tmin, tmax, lnB, soft, one, one)
     torch.cuda.synchronize(dev)
@@ -340,8 +343,9 @@ def grad_case(torch, dev, peaks, reps=3):
         torch.cuda.synchronize(dev)
         fwd.append(ev[0].elapsed_time(ev[1]))
         bwd.append(ev[1].elapsed_time(ev[2]))
-    cells = 256 * 1024 * 1024
-    out = {"workload": "256 templates x 2000 SFTs x 2 detectors (exp), 1024 t0 x 1024 tau "
+    cells = n_templates * 1024 * 1024
+    out = {"workload": f"{n_templates} templates x 2000 SFTs x 2 detectors (exp), 1024 t0 x "
+                       "1024 tau "
                        "(tau from 30075 s in steps of 1200 s), temperature 0.1",
            "cells": cells}
     for name, ms in (("forward", statistics.median(fwd)), ("backward", statistics.median(bwd))):
@@ -859,6 +863,17 @@ def main():
     if args.case == "single-480":
         if rank == 0:
             run_single_480(args)
+        return
+    if args.case == "grad":
+        if rank == 0:
+            import torch
+
+            from pyfstat_gb300 import _lib
+
+            peaks = _lib.probe_peaks(0)
+            g = grad_case(torch, torch.device("cuda", 0), peaks, reps=max(1, args.steps),
+                          n_templates=min(256, args.templates))
+            print(json.dumps({"case": "grad", **g}), flush=True)
         return
     if args.case:
         if rank == 0:

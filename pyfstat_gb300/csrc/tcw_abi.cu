@@ -1169,9 +1169,8 @@ static int diff_prepare(tcw_handle *h, const tcw_diff_desc *desc, uint32_t n,
                     ? L.add(sizeof(float) * TCW_DIFF_SLOTS * 128u * (size_t)max_rows * S.n_blocks)
                     : 0;
   S.o_D64 = pass == 1 ? L.add(sizeof(double) * 8u * std::max<uint64_t>(1, p_rows)) : 0;
-  // forward: the exponential templates' atoms in 32-byte rows, at their own row index
-  S.o_A8 = (pass == 0 && S.n_items) ? L.add(sizeof(float) * 8u * std::max<uint64_t>(1, atom_rows))
-                                    : 0;
+  // the exponential templates' atoms in 32-byte rows, at their own row index
+  S.o_A8 = S.n_items ? L.add(sizeof(float) * 8u * std::max<uint64_t>(1, atom_rows)) : 0;
   S.total = L.total;
   int rc = ensure_ws(h, S.total);
   if (rc) return rc;

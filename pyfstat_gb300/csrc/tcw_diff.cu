@@ -10,18 +10,22 @@
 // weights are differentiated (the boundaries are piecewise constant).
 //
 // At T = 0.1 the soft-max weights are exp(20 F), so a gradient good to 1e-4
-// needs F to ~1e-9 of its value: this path recomputes the window sums with
-// FP64 recurrences and F in FP64 (the map path stays FP32 / double-word).
+// needs F to ~1e-9 of its value.  The exponential windows' sums slide down
+// each tau column in double-word FP32 (ExpColumn, the map kernels'
+// arithmetic, ~1e-14 of the sums' magnitude) rather than in FP64, whose rate
+// on GB300 is 1/70 of FP32; F, its derivatives and the log-sum-exps are FP64
+// for the cells that carry weight (an FP32 tier-1 F far enough below the
+// maximum or the normaliser skips a cell, whose weight is then below e^-40):
 //
-//   pass A (diff_kernel<0>)  per tau column, rows descending: E(j) = x_j +
-//            r E(j+1) for both window edges, F in FP64, online log-sum-exp of
-//            F and 2F/T -> per-tile partials -> finalize per template.
-//   pass B (diff_kernel<1>)  the same walk plus the tau-derivative sums
-//            V(j) = r (V(j+1) + E(j+1)); per cell the adjoint sources
-//            G_c = g dF/dW_c (g = dL/dF) go to per-block scratch (no map is
-//            kept) and g dF/dtau accumulates per column;
-//   pass C (same kernel)     per column, atoms ascending, the transposed
-//            recurrence H(i) = r H(i-1) + sum_{lo(m)=i} G(m)
+//   diff_fwd_kernel  per tau column, rows descending: double-word window
+//            sums, FP64 log-sum-exps of F and 2F/T -> per-tile partials ->
+//            finalize per template.
+//   diff_bwd_kernel  pass B: the same walk plus the tau-derivative sums
+//            V = sum (i - lo) x r^(i - lo) (ExpColumnV); per cell the adjoint
+//            sources G_c = g dF/dW_c (g = dL/dF) go to per-block scratch (no
+//            map is kept) and g dF/dtau accumulates per column;
+//            pass C (same kernel): per column, atoms ascending, the
+//            transposed recurrence H(i) = r H(i-1) + sum_{lo(m)=i} G(m)
 //            - sum_{hi(m)+1=i} G(m) r^(L(m)) gives dL/dx(i) = H(i); columns
 //            are reduced across the block and added to the atom gradient.
 // The window-sum factor e^(-k (t_lo - t0)/tau) is left out everywhere: F does
@@ -136,273 +140,6 @@ constexpr uint32_t kDiffSlots = TCW_DIFF_SLOTS;
 constexpr int diff_min_blocks(int pass) {
   return pass == 0 ? TCW_DIFF_MIN_BLOCKS_FWD : TCW_DIFF_MIN_BLOCKS_BWD;
 }
-
-template <int kPass>
-__global__ void __launch_bounds__(kDiffBlock, diff_min_blocks(kPass))
-    diff_kernel(const DiffTemplate *__restrict__ T, const DiffItem *__restrict__ items,
-                uint32_t n_items, uint32_t *__restrict__ counter, const float *__restrict__ atoms,
-                const uint32_t *__restrict__ t0s_all, double temp, DiffPartial *__restrict__ parts,
-                const double *__restrict__ lnZ1, const double *__restrict__ lnZ2,
-                const double *__restrict__ gB, const double *__restrict__ gS,
-                float *__restrict__ scratch, uint32_t scratch_rows,
-                double *__restrict__ grad_atoms, double *__restrict__ grad_tau) {
-  __shared__ uint32_t s_item;
-  __shared__ double sh[kDiffBlock / 32][8];
-  __shared__ uint32_t s_end;
-  float *my_scratch = scratch ? scratch + (size_t)blockIdx.x * scratch_rows * kDiffSlots * kDiffBlock
-                              : nullptr;
-  for (;;) {
-    if (threadIdx.x == 0) s_item = atomicAdd(counter, 1u);
-    __syncthreads();
-    const uint32_t it = s_item;
-    __syncthreads();
-    if (it >= n_items) break;
-    const DiffItem w = items[it];
-    const DiffTemplate t = T[w.tmpl];
-    const uint32_t n = w.n0 + threadIdx.x;
-    const bool active = n < w.n1;
-    const uint32_t *t0s = t0s_all + t.t0_off;
-    const float *x = atoms + t.atom_off * 7u;
-    const double tau = tau_of(t, active ? n : w.n0);
-    const double r1 = exp(-(double)t.g.TAtom / tau), r2 = r1 * r1;
-    double rk[7];
-#pragma unroll
-    for (int c = 0; c < 7; c++) rk[c] = c < 3 ? r2 : r1;
-    const double inv_r1 = r1 > 1e-280 ? 1.0 / r1 : 0.0;
-    // online log-sum-exp (pass A) / tau gradient (pass B)
-    double m1 = -INFINITY, s1 = 0.0, m2 = -INFINITY, s2 = 0.0, dtau = 0.0;
-    double z1 = 0.0, z2 = 0.0, gb = 0.0, gs = 0.0;
-    if (kPass == 1) {
-      // normalisers from the forward outputs: logsumexp F and logsumexp 2F/T
-      z1 = lnZ1[w.tmpl] - log(70.0 / ((double)t.N_t0 * (double)t.N_tau));
-      z2 = lnZ2[w.tmpl] / temp;
-      gb = gB[w.tmpl];
-      gs = gS[w.tmpl];
-    }
-    if (active) {
-      double Elo[7], Ehi[7], Vlo[7], Vhi[7];
-#pragma unroll
-      for (int c = 0; c < 7; c++) Elo[c] = Ehi[c] = Vlo[c] = Vhi[c] = 0.0;
-      uint32_t J = 0, jL = 0, jH = 0, nz = 0xFFFFFFFFu, Lp = 0;
-      double pw = 1.0;
-      bool init = false;
-      for (uint32_t mm = t.N_t0; mm > 0; mm--) {
-        const uint32_t m = mm - 1u;
-        const uint32_t t0 = __ldg(t0s + m);
-        const uint32_t lo = exp_lo(t0, t.g);
-        uint32_t hi = 0;
-        const bool nonempty = exp_hi_real(t0, tau, t.g, hi) && lo <= hi;
-        double G[7] = {0, 0, 0, 0, 0, 0, 0};
-        float p1h = 0.0f, p1l = 0.0f;
-        double F = 2.0;
-        if (nonempty) {
-          const uint32_t top = hi + 1u;
-          if (!init || top > J || lo > jL || top > jH) {
-            J = jL = jH = top;
-            nz = 0xFFFFFFFFu;
-#pragma unroll
-            for (int c = 0; c < 7; c++) Elo[c] = Ehi[c] = Vlo[c] = Vhi[c] = 0.0;
-            init = true;
-          }
-          while (jH > top) {
-            jH--;
-            TCW_DCHECK(jH < t.g.numAtoms);
-#pragma unroll
-            for (int c = 0; c < 7; c++) {
-              const double xv = (double)__ldg(x + (size_t)jH * 7u + c);
-              if (kPass == 1) Vhi[c] = rk[c] * (Vhi[c] + Ehi[c]);
-              Ehi[c] = fma(rk[c], Ehi[c], xv);
-            }
-          }
-          while (jL > lo) {
-            jL--;
-            TCW_DCHECK(jL < t.g.numAtoms);
-            const float a2 = __ldg(x + (size_t)jL * 7u), b2 = __ldg(x + (size_t)jL * 7u + 1u);
-#pragma unroll
-            for (int c = 0; c < 7; c++) {
-              const double xv = (double)__ldg(x + (size_t)jL * 7u + c);
-              if (kPass == 1) Vlo[c] = rk[c] * (Vlo[c] + Elo[c]);
-              Elo[c] = fma(rk[c], Elo[c], xv);
-            }
-            if (a2 != 0.0f || b2 != 0.0f) nz = jL;
-          }
-          if (nz <= hi) {
-            const uint32_t L = top - lo;
-            if (L != Lp) {
-              if (L == Lp + 1u)
-                pw *= r1;
-              else if (L + 1u == Lp && inv_r1 > 0.0)
-                pw *= inv_r1;
-              else
-                pw = pow(r1, (double)L);
-              Lp = L;
-            }
-            const double p2 = pw * pw;
-            double W[7], V[7];
-#pragma unroll
-            for (int c = 0; c < 7; c++) {
-              const double pk = c < 3 ? p2 : pw;
-              W[c] = Elo[c] - pk * Ehi[c];
-              if (kPass == 1) V[c] = Vlo[c] - pk * (Vhi[c] + (double)L * Ehi[c]);
-            }
-            const F64Cell fc = fstat64(W);
-            F = fc.F;
-            if (kPass == 1 && fc.ok) {
-              const double g = gb * (double)exp2f((float)(F - z1) * kLog2eF) +
-                               gs * 2.0 * (double)exp2f((float)(2.0 * F / temp - z2) * kLog2eF);
-              const double A = W[0], B = W[1], C = W[2], iD = 1.0 / fc.D;
-              const double Fa2 = W[3] * W[3] + W[4] * W[4], Fb2 = W[5] * W[5] + W[6] * W[6];
-              const double re = W[3] * W[5] + W[4] * W[6];
-              double dF[7];
-              dF[0] = (Fb2 - F * B) * iD;
-              dF[1] = (Fa2 - F * A) * iD;
-              dF[2] = (2.0 * F * C - 2.0 * re) * iD;
-              dF[3] = 2.0 * (B * W[3] - C * W[5]) * iD;
-              dF[4] = 2.0 * (B * W[4] - C * W[6]) * iD;
-              dF[5] = 2.0 * (A * W[5] - C * W[3]) * iD;
-              dF[6] = 2.0 * (A * W[6] - C * W[4]) * iD;
-#pragma unroll
-              for (int c = 0; c < 7; c++) {
-                G[c] = g * dF[c];
-                dtau += G[c] * (c < 3 ? 2.0 : 1.0) * V[c];
-              }
-              p1h = (float)pw;
-              p1l = (float)(pw - (double)p1h);
-            }
-          }
-        }
-        if (kPass == 0) {
-          lse_add(m1, s1, F);
-          lse_add(m2, s2, 2.0 * F / temp);
-        } else {
-          TCW_DCHECK(m < scratch_rows);
-          float *sc = my_scratch + (size_t)m * kDiffSlots * kDiffBlock + threadIdx.x;
-#pragma unroll
-          for (int c = 0; c < 7; c++) sc[(size_t)c * kDiffBlock] = (float)G[c];
-          sc[(size_t)7 * kDiffBlock] = p1h;
-          sc[(size_t)8 * kDiffBlock] = p1l;
-        }
-      }
-    }
-    if (kPass == 0) {
-      // block merge of the two log-sum-exp pairs (warp shuffles, then smem)
-#pragma unroll
-      for (int d = 16; d > 0; d >>= 1) {
-        const double om1 = __shfl_down_sync(0xffffffffu, m1, d);
-        const double os1 = __shfl_down_sync(0xffffffffu, s1, d);
-        const double om2 = __shfl_down_sync(0xffffffffu, m2, d);
-        const double os2 = __shfl_down_sync(0xffffffffu, s2, d);
-        lse_merge(m1, s1, om1, os1);
-        lse_merge(m2, s2, om2, os2);
-      }
-      if ((threadIdx.x & 31u) == 0) {
-        sh[threadIdx.x >> 5][0] = m1;
-        sh[threadIdx.x >> 5][1] = s1;
-        sh[threadIdx.x >> 5][2] = m2;
-        sh[threadIdx.x >> 5][3] = s2;
-      }
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        for (int k = 1; k < kDiffBlock / 32; k++) {
-          lse_merge(m1, s1, sh[k][0], sh[k][1]);
-          lse_merge(m2, s2, sh[k][2], sh[k][3]);
-        }
-        parts[w.part] = DiffPartial{m1, s1, m2, s2};
-      }
-      __syncthreads();
-      continue;
-    }
-
-    // ---- pass B done for this tile: tau gradient, then pass C (ascending)
-    __syncthreads();  // scratch of all columns written
-    const double scale = active ? (double)t.g.TAtom / (tau * tau) * dtau : 0.0;
-    const double fr = (active && t.N_tau > 1) ? (double)n / (double)(t.N_tau - 1u) : 0.0;
-    double dmax = scale * fr, dmin = scale * (active && t.N_tau > 1 ? 1.0 - fr : (active ? 1.0 : 0.0));
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) {
-      dmax += __shfl_down_sync(0xffffffffu, dmax, d);
-      dmin += __shfl_down_sync(0xffffffffu, dmin, d);
-    }
-    if ((threadIdx.x & 31u) == 0) {
-      sh[threadIdx.x >> 5][0] = dmin;
-      sh[threadIdx.x >> 5][1] = dmax;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double a = 0.0, b = 0.0;
-      for (int k = 0; k < kDiffBlock / 32; k++) {
-        a += sh[k][0];
-        b += sh[k][1];
-      }
-      atomicAdd(grad_tau + 2u * w.tmpl, a);
-      atomicAdd(grad_tau + 2u * w.tmpl + 1u, b);
-      s_end = 0;
-    }
-    __syncthreads();
-    // atom range of the transposed recurrence: from the first row's window
-    // start to the largest window end of the tile
-    const uint32_t i_begin = exp_lo(__ldg(t0s), t.g);
-    uint32_t my_end = i_begin;
-    if (active) {
-      uint32_t hi;
-      if (exp_hi_real(__ldg(t0s + t.N_t0 - 1u), tau, t.g, hi)) my_end = hi + 1u;
-    }
-    atomicMax(&s_end, my_end);
-    __syncthreads();
-    const uint32_t i_end = s_end;
-    double H[7] = {0, 0, 0, 0, 0, 0, 0};
-    uint32_t mi = 0, mr = 0;
-    uint32_t lo_next = exp_lo(__ldg(t0s), t.g);
-    const float *sc0 = my_scratch + threadIdx.x;
-    for (uint32_t i = i_begin; i < i_end; i++) {
-      if (active) {
-#pragma unroll
-        for (int c = 0; c < 7; c++) H[c] *= rk[c];
-        while (mi < t.N_t0 && lo_next <= i) {
-          const float *sc = sc0 + (size_t)mi * kDiffSlots * kDiffBlock;
-#pragma unroll
-          for (int c = 0; c < 7; c++) H[c] += (double)sc[(size_t)c * kDiffBlock];
-          mi++;
-          if (mi < t.N_t0) lo_next = exp_lo(__ldg(t0s + mi), t.g);
-        }
-        while (mr < mi) {
-          const uint32_t t0 = __ldg(t0s + mr);
-          uint32_t hi;
-          const uint32_t lo = exp_lo(t0, t.g);
-          uint32_t end = lo;  // empty windows: removal right after injection
-          if (exp_hi_real(t0, tau, t.g, hi) && lo <= hi) end = hi + 1u;
-          if (end > i) break;
-          const float *sc = sc0 + (size_t)mr * kDiffSlots * kDiffBlock;
-          const double p1 = (double)sc[(size_t)7 * kDiffBlock] + (double)sc[(size_t)8 * kDiffBlock];
-          const double p2 = p1 * p1;
-#pragma unroll
-          for (int c = 0; c < 7; c++) H[c] -= (double)sc[(size_t)c * kDiffBlock] * (c < 3 ? p2 : p1);
-          mr++;
-        }
-      }
-      // reduce the columns' contributions to atom i
-      double v[7];
-#pragma unroll
-      for (int c = 0; c < 7; c++) {
-        v[c] = active ? H[c] : 0.0;
-#pragma unroll
-        for (int d = 16; d > 0; d >>= 1) v[c] += __shfl_down_sync(0xffffffffu, v[c], d);
-      }
-      if ((threadIdx.x & 31u) == 0) {
-#pragma unroll
-        for (int c = 0; c < 7; c++) sh[threadIdx.x >> 5][c] = v[c];
-      }
-      __syncthreads();
-      if (threadIdx.x < 7u && i < t.g.numAtoms) {
-        double a = 0.0;
-        for (int k = 0; k < kDiffBlock / 32; k++) a += sh[k][threadIdx.x];
-        if (a != 0.0) atomicAdd(grad_atoms + (t.atom_off + i) * 7u + threadIdx.x, a);
-      }
-      __syncthreads();
-    }
-  }
-}
-
 
 // ------------------------------------------------------------ exponential forward (double-word)
 
@@ -647,6 +384,275 @@ struct ExpColumnV {
   }
 };
 
+// Backward pass of exponential windows.  Pass B slides W and V down each
+// tau column in double-word FP32 (ExpColumnV) with the per-row quantities
+// tabulated per warp; a cell gets FP64 F, dF/dW and its adjoint sources only
+// when it carries weight.  Its weight g = gB e^(F - Z1) + 2 gS e^(2F/T - Z2)
+// (Z1 = logsumexp F, Z2 = logsumexp 2F/T, from the forward outputs) is below
+// e^-40 when the FP32 tier-1 F (good to ~1e-5 of F) lies more than 42 below
+// Z1 (the lnBtSG term, gB != 0) and more than 40 T + 1 below (T/2) Z2 (the
+// soft-max term, gS != 0: its exponent is then below -80); such cells
+// contribute no sources.  Pass C (the transposed recurrence) runs in FP64, with the window
+// ends of regular rows from the integer split.
+__global__ void __launch_bounds__(kDiffBlock, diff_min_blocks(1))
+    diff_bwd_kernel(const DiffTemplate *__restrict__ T, const DiffItem *__restrict__ items,
+                    uint32_t n_items, uint32_t *__restrict__ counter,
+                    const float *__restrict__ atoms8, const uint32_t *__restrict__ t0s_all,
+                    double temp, const double *__restrict__ lnZ1, const double *__restrict__ lnZ2,
+                    const double *__restrict__ gB, const double *__restrict__ gS,
+                    float *__restrict__ scratch, uint32_t scratch_rows,
+                    double *__restrict__ grad_atoms, double *__restrict__ grad_tau) {
+  __shared__ uint32_t s_item;
+  __shared__ double sh[kDiffBlock / 32][8];
+  __shared__ uint32_t s_end;
+  __shared__ __align__(16) ExpRow s_tab[kDiffBlock / 32][kDiffRowTab];
+  const uint32_t lane = threadIdx.x & 31u;
+  ExpRow *tab = s_tab[threadIdx.x >> 5];
+  float *my_scratch = scratch + (size_t)blockIdx.x * scratch_rows * kDiffSlots * kDiffBlock;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(counter, 1u);
+    __syncthreads();
+    const uint32_t it = s_item;
+    __syncthreads();
+    if (it >= n_items) break;
+    const DiffItem w = items[it];
+    const DiffTemplate t = T[w.tmpl];
+    const uint32_t n = w.n0 + threadIdx.x;
+    const bool active = n < w.n1;
+    const uint32_t *t0s = t0s_all + t.t0_off;
+    const float *a8 = atoms8 + t.atom_off * 8u;
+    const uint32_t *a8u = reinterpret_cast<const uint32_t *>(a8);
+    const double tau = tau_of(t, active ? n : w.n0);
+    const double r1 = exp(-(double)t.g.TAtom / tau);
+    const double inv_r1 = r1 > 1e-280 ? 1.0 / r1 : 0.0;
+    // normalisers from the forward outputs: logsumexp F and logsumexp 2F/T
+    const double z1 = lnZ1[w.tmpl] - log(70.0 / ((double)t.N_t0 * (double)t.N_tau));
+    const double z2 = lnZ2[w.tmpl] / temp;
+    const double gb = gB[w.tmpl], gs = gS[w.tmpl];
+    // a tier-1 F below `skip` carries no weight in either sum
+    const double sk1 = gb != 0.0 ? z1 - 42.0 : INFINITY;
+    const double sk2 = gs != 0.0 ? 0.5 * temp * (z2 - 80.0) - 1.0 : INFINITY;
+    const float skip = (float)fmin(sk1, sk2);
+    const uint32_t tau_up = !active ? 0u
+                            : (tau >= 4294967295.0 ? 0xFFFFFFFFu : (uint32_t)ceil(tau));
+    const uint32_t taumax = __reduce_max_sync(0xffffffffu, tau_up);
+    ExpColumnV CV;
+    CV.C.init_real(t.g, tau);
+    CV.reset_v();
+    double dtau = 0.0, pw64 = 1.0;
+    uint32_t Lp64 = 0;
+    for (uint32_t ce = t.N_t0; ce > 0;) {
+      const uint32_t cb = ce > kDiffRowTab ? ce - kDiffRowTab : 0u;
+      bool reg = true;
+      for (uint32_t r = lane; r < ce - cb; r += 32u)
+        reg = reg && exp_row_regular(__ldg(t0s + cb + r), taumax, t.g);
+      reg = __all_sync(0xffffffffu, reg);
+      __syncwarp();
+      for (uint32_t r = lane; r < ce - cb; r += 32u) {
+        const uint32_t t0 = __ldg(t0s + cb + r);
+        ExpRow e;
+        e.lo = exp_lo(t0, t.g);
+        e.nz = e.lo < t.g.numAtoms ? __ldg(a8u + (size_t)e.lo * 8u + 3u) : 0xFFFFFFFFu;
+        const uint32_t d = t0 - t.g.t0_data;
+        e.a = reg ? fdiv(d, t.g.div) : t0;  // irregular chunks: the generic branch reads t0
+        e.b = reg ? d - e.a * t.g.TAtom : 0u;
+        tab[r] = e;
+      }
+      __syncwarp();
+      if (active) {
+        for (uint32_t m = ce; m > cb;) {
+          m--;
+          const ExpRow e = tab[m - cb];
+          uint32_t top = 0;
+          bool data = false;
+          if (reg) {
+            const uint32_t v = e.b + CV.C.RmT;
+            top = e.a + CV.C.Qp1 - (v >> 31);
+            top = top < 1u ? 1u : (top < t.g.numAtoms ? top : t.g.numAtoms);
+            data = e.lo < top && CV.slide(a8, t.g, e.lo, top, e.nz);
+          } else {
+            uint32_t hi;
+            if (exp_hi_real(e.a, tau, t.g, hi) && e.lo <= hi) {
+              top = hi + 1u;
+              data = CV.slide(a8, t.g, e.lo, top, e.nz);
+            }
+          }
+          double G[7] = {0, 0, 0, 0, 0, 0, 0};
+          float p1h = 0.0f, p1l = 0.0f;
+          if (data) {
+            // r^L, L = top - lo, for the removal in the transposed recurrence
+            // (FP64, one multiplication when L moves by one)
+            const uint32_t L = top - e.lo;
+            if (L != Lp64) {
+              if (L == Lp64 + 1u)
+                pw64 *= r1;
+              else if (L + 1u == Lp64 && inv_r1 > 0.0)
+                pw64 *= inv_r1;
+              else
+                pw64 = pow(r1, (double)L);
+              Lp64 = L;
+            }
+            const ExpColumn<false> &C = CV.C;
+            float F32;
+            const F2 s0 = add2(C.W0.h, C.W0.l), s2v = add2(C.W2.h, C.W2.l),
+                     s3 = add2(C.W3.h, C.W3.l);
+            const float sc = fadd(C.Wc.h, C.Wc.l);
+            const bool t1 = fstat_fast_sums(s0.x, s0.y, sc, s2v.x, s2v.y, s3.x, s3.y, F32);
+            if (!(t1 && F32 < skip)) {
+              double W[7];
+              W[0] = dw_value(C.W0.h.x, C.W0.l.x);
+              W[1] = dw_value(C.W0.h.y, C.W0.l.y);
+              W[2] = dw_value(C.Wc.h, C.Wc.l);
+              W[3] = dw_value(C.W2.h.x, C.W2.l.x);
+              W[4] = dw_value(C.W2.h.y, C.W2.l.y);
+              W[5] = dw_value(C.W3.h.x, C.W3.l.x);
+              W[6] = dw_value(C.W3.h.y, C.W3.l.y);
+              const F64Cell fc = fstat64(W);
+              if (fc.ok) {
+                double V[7];
+                V[0] = dw_value(CV.V0.h.x, CV.V0.l.x);
+                V[1] = dw_value(CV.V0.h.y, CV.V0.l.y);
+                V[2] = dw_value(CV.Vc.h, CV.Vc.l);
+                V[3] = dw_value(CV.V2.h.x, CV.V2.l.x);
+                V[4] = dw_value(CV.V2.h.y, CV.V2.l.y);
+                V[5] = dw_value(CV.V3.h.x, CV.V3.l.x);
+                V[6] = dw_value(CV.V3.h.y, CV.V3.l.y);
+                const double F = fc.F;
+                const double g = gb * (double)exp2f((float)(F - z1) * kLog2eF) +
+                                 gs * 2.0 * (double)exp2f((float)(2.0 * F / temp - z2) * kLog2eF);
+                const double A = W[0], B = W[1], Cc = W[2], iD = 1.0 / fc.D;
+                const double Fa2 = W[3] * W[3] + W[4] * W[4], Fb2 = W[5] * W[5] + W[6] * W[6];
+                const double re = W[3] * W[5] + W[4] * W[6];
+                double dF[7];
+                dF[0] = (Fb2 - F * B) * iD;
+                dF[1] = (Fa2 - F * A) * iD;
+                dF[2] = (2.0 * F * Cc - 2.0 * re) * iD;
+                dF[3] = 2.0 * (B * W[3] - Cc * W[5]) * iD;
+                dF[4] = 2.0 * (B * W[4] - Cc * W[6]) * iD;
+                dF[5] = 2.0 * (A * W[5] - Cc * W[3]) * iD;
+                dF[6] = 2.0 * (A * W[6] - Cc * W[4]) * iD;
+#pragma unroll
+                for (int c = 0; c < 7; c++) {
+                  G[c] = g * dF[c];
+                  dtau += G[c] * (c < 3 ? 2.0 : 1.0) * V[c];
+                }
+                p1h = (float)pw64;
+                p1l = (float)(pw64 - (double)p1h);
+              }
+            }
+          }
+          TCW_DCHECK(m < scratch_rows);
+          float *scr = my_scratch + (size_t)m * kDiffSlots * kDiffBlock + threadIdx.x;
+#pragma unroll
+          for (int c = 0; c < 7; c++) scr[(size_t)c * kDiffBlock] = (float)G[c];
+          scr[(size_t)7 * kDiffBlock] = p1h;
+          scr[(size_t)8 * kDiffBlock] = p1l;
+        }
+      }
+      ce = cb;
+    }
+
+    // ---- pass B done for this tile: tau gradient, then pass C (ascending)
+    __syncthreads();  // scratch of all columns written
+    const double scale = active ? (double)t.g.TAtom / (tau * tau) * dtau : 0.0;
+    const double fr = (active && t.N_tau > 1) ? (double)n / (double)(t.N_tau - 1u) : 0.0;
+    double dmax = scale * fr,
+           dmin = scale * (active && t.N_tau > 1 ? 1.0 - fr : (active ? 1.0 : 0.0));
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+      dmax += __shfl_down_sync(0xffffffffu, dmax, d);
+      dmin += __shfl_down_sync(0xffffffffu, dmin, d);
+    }
+    if (lane == 0) {
+      sh[threadIdx.x >> 5][0] = dmin;
+      sh[threadIdx.x >> 5][1] = dmax;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double a = 0.0, b = 0.0;
+      for (int k = 0; k < kDiffBlock / 32; k++) {
+        a += sh[k][0];
+        b += sh[k][1];
+      }
+      atomicAdd(grad_tau + 2u * w.tmpl, a);
+      atomicAdd(grad_tau + 2u * w.tmpl + 1u, b);
+      s_end = 0;
+    }
+    __syncthreads();
+    // one past the window end of row m (the window start for empty windows:
+    // removal right after injection), from the integer split on regular
+    // rows, else from the real t1
+    auto row_end = [&](uint32_t m) -> uint32_t {
+      const uint32_t t0 = __ldg(t0s + m);
+      const uint32_t lo = exp_lo(t0, t.g);
+      if (exp_row_regular(t0, taumax, t.g)) {
+        const uint32_t dd = t0 - t.g.t0_data;
+        const uint32_t a = fdiv(dd, t.g.div), b = dd - a * t.g.TAtom;
+        uint32_t top = a + CV.C.Qp1 - ((b + CV.C.RmT) >> 31);
+        top = top < 1u ? 1u : (top < t.g.numAtoms ? top : t.g.numAtoms);
+        return lo < top ? top : lo;
+      }
+      uint32_t hi;
+      return (exp_hi_real(t0, tau, t.g, hi) && lo <= hi) ? hi + 1u : lo;
+    };
+    // atom range of the transposed recurrence: from the first row's window
+    // start to the largest window end of the tile
+    const uint32_t i_begin = exp_lo(__ldg(t0s), t.g);
+    atomicMax(&s_end, active ? row_end(t.N_t0 - 1u) : i_begin);
+    __syncthreads();
+    const uint32_t i_end = s_end;
+    const double rk2 = r1 * r1;
+    double H[7] = {0, 0, 0, 0, 0, 0, 0};
+    uint32_t mi = 0, mr = 0;
+    uint32_t lo_next = i_begin;
+    uint32_t end_r = active ? row_end(0) : 0u;
+    const float *sc0 = my_scratch + threadIdx.x;
+    for (uint32_t i = i_begin; i < i_end; i++) {
+      if (active) {
+#pragma unroll
+        for (int c = 0; c < 7; c++) H[c] *= (c < 3 ? rk2 : r1);
+        while (mi < t.N_t0 && lo_next <= i) {
+          const float *scr = sc0 + (size_t)mi * kDiffSlots * kDiffBlock;
+#pragma unroll
+          for (int c = 0; c < 7; c++) H[c] += (double)scr[(size_t)c * kDiffBlock];
+          mi++;
+          if (mi < t.N_t0) lo_next = exp_lo(__ldg(t0s + mi), t.g);
+        }
+        while (mr < mi && end_r <= i) {
+          const float *scr = sc0 + (size_t)mr * kDiffSlots * kDiffBlock;
+          const double p1 =
+              (double)scr[(size_t)7 * kDiffBlock] + (double)scr[(size_t)8 * kDiffBlock];
+          const double p2 = p1 * p1;
+#pragma unroll
+          for (int c = 0; c < 7; c++)
+            H[c] -= (double)scr[(size_t)c * kDiffBlock] * (c < 3 ? p2 : p1);
+          mr++;
+          if (mr < t.N_t0) end_r = row_end(mr);
+        }
+      }
+      // reduce the columns' contributions to atom i
+      double v[7];
+#pragma unroll
+      for (int c = 0; c < 7; c++) {
+        v[c] = active ? H[c] : 0.0;
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) v[c] += __shfl_down_sync(0xffffffffu, v[c], d);
+      }
+      if (lane == 0) {
+#pragma unroll
+        for (int c = 0; c < 7; c++) sh[threadIdx.x >> 5][c] = v[c];
+      }
+      __syncthreads();
+      if (threadIdx.x < 7u && i < t.g.numAtoms) {
+        double a = 0.0;
+        for (int k = 0; k < kDiffBlock / 32; k++) a += sh[k][threadIdx.x];
+        if (a != 0.0) atomicAdd(grad_atoms + (t.atom_off + i) * 7u + threadIdx.x, a);
+      }
+      __syncthreads();
+    }
+  }
+}
+
 // ------------------------------------------------------------ rectangular windows
 
 // Inclusive end index of a rectangular window for a real tau (the
@@ -844,7 +850,7 @@ int diff_blocks_per_sm(int pass) {
   int n = 0;
   cudaError_t e = pass == 0
                       ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, diff_fwd_kernel, kDiffBlock, 0)
-                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, diff_kernel<1>, kDiffBlock, 0);
+                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, diff_bwd_kernel, kDiffBlock, 0);
   if (e != cudaSuccess) {
     cudaGetLastError();
     n = 1;
@@ -871,10 +877,12 @@ cudaError_t launch_diff(int pass, const DiffLaunch &L, cudaStream_t stream) {
       diff_repack_kernel<<<L.n_exp, 256, 0, stream>>>(L.T, L.exp_list, L.atoms, L.atoms8);
       diff_fwd_kernel<<<L.n_blocks, kDiffBlock, 0, stream>>>(L.T, L.items, L.n_items, L.counter,
                                                              L.atoms8, L.t0s, L.temp, L.parts);
-    } else
-      diff_kernel<1><<<L.n_blocks, kDiffBlock, 0, stream>>>(
-          L.T, L.items, L.n_items, L.counter, L.atoms, L.t0s, L.temp, nullptr, L.lnZ1, L.lnZ2,
-          L.gB, L.gS, L.scratch, L.scratch_rows, L.grad_atoms, L.grad_tau);
+    } else {
+      diff_repack_kernel<<<L.n_exp, 256, 0, stream>>>(L.T, L.exp_list, L.atoms, L.atoms8);
+      diff_bwd_kernel<<<L.n_blocks, kDiffBlock, 0, stream>>>(
+          L.T, L.items, L.n_items, L.counter, L.atoms8, L.t0s, L.temp, L.lnZ1, L.lnZ2, L.gB,
+          L.gS, L.scratch, L.scratch_rows, L.grad_atoms, L.grad_tau);
+    }
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }

@@ -159,9 +159,9 @@ struct DiffLaunch {
   uint32_t n_items, n_blocks;
   uint32_t *counter;
   const float *atoms;
-  float *atoms8;                     // pass A: exponential templates' atoms in 32-byte rows
+  float *atoms8;                     // exponential templates' atoms in 32-byte rows
                                      // (same row index as `atoms`), written by the launch
-  const uint32_t *exp_list;          // pass A: the exponential templates' indices
+  const uint32_t *exp_list;          // the exponential templates' indices
   uint32_t n_exp;
   const uint32_t *t0s;
   double temp;
