@@ -149,9 +149,11 @@ constexpr int diff_min_blocks(int pass) {
 // window's magnitude, against FP64 recurrences at GB300's 1/70 FP64 rate),
 // with the per-row quantities tabulated per warp and the real tau's window
 // end split as in ExpColumn::init_real.  F goes into the FP64 log-sum-exps:
-// a cell whose FP32 tier-1 F lies more than 62 below the column's running
-// maximum carries exp(F - max) < e^-60 in both sums (the soft-max's
-// 2F/T - max is 2/T times lower still) and is skipped -- the tier-1 F is good
+// a cell whose FP32 tier-1 F lies more than 62 below a lower bound of the
+// template's maximum (the column's running maximum, or the tile's largest
+// tier-1 F found by a first, FP32-only sweep) carries exp(F - max) < e^-60
+// in both sums (the soft-max's 2F/T - max is 2/T times lower still) and is
+// skipped -- the tier-1 F is good
 // to ~1.5e-6 relative and passes only for cond < 32, where the FP64 test
 // passes too; every other cell gets F in FP64 from the double-word sums
 // (the reference's formula and conditioning test, fstat64).  Rows that are
@@ -208,60 +210,85 @@ __global__ void __launch_bounds__(kDiffBlock, diff_min_blocks(0))
     const uint32_t taumax = __reduce_max_sync(0xffffffffu, tau_up);
     ExpColumn<false> C;
     C.init_real(t.g, tau);
-    for (uint32_t ce = t.N_t0; ce > 0;) {
-      const uint32_t cb = ce > kDiffRowTab ? ce - kDiffRowTab : 0u;
-      bool reg = true;
-      for (uint32_t r = lane; r < ce - cb; r += 32u)
-        reg = reg && exp_row_regular(__ldg(t0s + cb + r), taumax, t.g);
-      reg = __all_sync(0xffffffffu, reg);
-      __syncwarp();
-      for (uint32_t r = lane; r < ce - cb; r += 32u) {
-        const uint32_t t0 = __ldg(t0s + cb + r);
-        ExpRow e;
-        e.lo = exp_lo(t0, t.g);
-        e.nz = e.lo < t.g.numAtoms ? __ldg(a8u + (size_t)e.lo * 8u + 3u) : 0xFFFFFFFFu;
-        const uint32_t d = t0 - t.g.t0_data;
-        e.a = reg ? fdiv(d, t.g.div) : t0;  // irregular chunks: the generic branch reads t0
-        e.b = reg ? d - e.a * t.g.TAtom : 0u;
-        tab[r] = e;
+    // Two sweeps down the columns: the first finds the tile's largest tier-1
+    // F (FP32 only), a lower bound of the template's maximum to within its
+    // ~1e-5 error, so that the second skips the cells 62 below it from the
+    // start instead of only below the running maximum.
+    float est = -INFINITY, skip0 = -INFINITY;
+    for (int sweep = 0; sweep < 2; sweep++) {
+      if (sweep == 1) {
+        float v = est;
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, d));
+        if (lane == 0) sh[threadIdx.x >> 5][0] = (double)v;
+        __syncthreads();
+        double tile = sh[0][0];
+        for (int k = 1; k < kDiffBlock / 32; k++) tile = fmax(tile, sh[k][0]);
+        __syncthreads();
+        if (tile > -INFINITY) skip0 = (float)(tile - 1e-5 * fabs(tile) - 63.0);
+        skip = skip0;
+        C.reset();
       }
-      __syncwarp();
-      if (active) {
-        for (uint32_t m = ce; m > cb;) {
-          m--;
-          const ExpRow e = tab[m - cb];
-          bool data;
-          if (reg) {
-            data = C.window(a8, t.g, e);
-          } else {  // the window end from the real t1 (e.a holds t0 on these rows)
-            uint32_t hi;
-            data = exp_hi_real(e.a, tau, t.g, hi) && e.lo <= hi &&
-                   C.slide(a8, t.g, e.lo, hi + 1u, e.nz);
-          }
-          double F = 2.0;
-          if (data) {
-            float F32;
-            const F2 s0 = add2(C.W0.h, C.W0.l), s2v = add2(C.W2.h, C.W2.l),
-                     s3 = add2(C.W3.h, C.W3.l);
-            const float sc = fadd(C.Wc.h, C.Wc.l);
-            if (fstat_fast_sums(s0.x, s0.y, sc, s2v.x, s2v.y, s3.x, s3.y, F32) && F32 < skip)
-              continue;
-            double W[7];
-            W[0] = (double)C.W0.h.x + (double)C.W0.l.x;
-            W[1] = (double)C.W0.h.y + (double)C.W0.l.y;
-            W[2] = (double)C.Wc.h + (double)C.Wc.l;
-            W[3] = (double)C.W2.h.x + (double)C.W2.l.x;
-            W[4] = (double)C.W2.h.y + (double)C.W2.l.y;
-            W[5] = (double)C.W3.h.x + (double)C.W3.l.x;
-            W[6] = (double)C.W3.h.y + (double)C.W3.l.y;
-            F = fstat64(W).F;
-          } else if (2.0f < skip) {
-            continue;
-          }
-          lse_pair_add(m1, s1, m2, s2, F, temp, skip);
+      for (uint32_t ce = t.N_t0; ce > 0;) {
+        const uint32_t cb = ce > kDiffRowTab ? ce - kDiffRowTab : 0u;
+        bool reg = true;
+        for (uint32_t r = lane; r < ce - cb; r += 32u)
+          reg = reg && exp_row_regular(__ldg(t0s + cb + r), taumax, t.g);
+        reg = __all_sync(0xffffffffu, reg);
+        __syncwarp();
+        for (uint32_t r = lane; r < ce - cb; r += 32u) {
+          const uint32_t t0 = __ldg(t0s + cb + r);
+          ExpRow e;
+          e.lo = exp_lo(t0, t.g);
+          e.nz = e.lo < t.g.numAtoms ? __ldg(a8u + (size_t)e.lo * 8u + 3u) : 0xFFFFFFFFu;
+          const uint32_t d = t0 - t.g.t0_data;
+          e.a = reg ? fdiv(d, t.g.div) : t0;  // irregular chunks: the generic branch reads t0
+          e.b = reg ? d - e.a * t.g.TAtom : 0u;
+          tab[r] = e;
         }
+        __syncwarp();
+        if (active) {
+          for (uint32_t m = ce; m > cb;) {
+            m--;
+            const ExpRow e = tab[m - cb];
+            bool data;
+            if (reg) {
+              data = C.window(a8, t.g, e);
+            } else {  // the window end from the real t1 (e.a holds t0 on these rows)
+              uint32_t hi;
+              data = exp_hi_real(e.a, tau, t.g, hi) && e.lo <= hi &&
+                     C.slide(a8, t.g, e.lo, hi + 1u, e.nz);
+            }
+            double F = 2.0;
+            if (data) {
+              float F32;
+              const F2 s0 = add2(C.W0.h, C.W0.l), s2v = add2(C.W2.h, C.W2.l),
+                       s3 = add2(C.W3.h, C.W3.l);
+              const float sc = fadd(C.Wc.h, C.Wc.l);
+              const bool t1 = fstat_fast_sums(s0.x, s0.y, sc, s2v.x, s2v.y, s3.x, s3.y, F32);
+              if (sweep == 0) {
+                if (t1) est = fmaxf(est, F32);
+                continue;
+              }
+              if (t1 && F32 < skip) continue;
+              double W[7];
+              W[0] = (double)C.W0.h.x + (double)C.W0.l.x;
+              W[1] = (double)C.W0.h.y + (double)C.W0.l.y;
+              W[2] = (double)C.Wc.h + (double)C.Wc.l;
+              W[3] = (double)C.W2.h.x + (double)C.W2.l.x;
+              W[4] = (double)C.W2.h.y + (double)C.W2.l.y;
+              W[5] = (double)C.W3.h.x + (double)C.W3.l.x;
+              W[6] = (double)C.W3.h.y + (double)C.W3.l.y;
+              F = fstat64(W).F;
+            } else if (sweep == 0 || 2.0f < skip) {
+              continue;
+            }
+            lse_pair_add(m1, s1, m2, s2, F, temp, skip);
+            skip = fmaxf(skip, skip0);
+          }
+        }
+        ce = cb;
       }
-      ce = cb;
     }
     // block merge of the two log-sum-exp pairs (warp shuffles, then smem)
 #pragma unroll
