@@ -657,26 +657,23 @@ __global__ void __launch_bounds__(kDiffBlock, diff_min_blocks(1))
           if (mr < t.N_t0) end_r = row_end(mr);
         }
       }
-      // reduce the columns' contributions to atom i
+      // reduce the warp's columns' contributions to atom i; each warp adds its
+      // own (no block barrier per atom)
       double v[7];
 #pragma unroll
       for (int c = 0; c < 7; c++) {
         v[c] = active ? H[c] : 0.0;
 #pragma unroll
-        for (int d = 16; d > 0; d >>= 1) v[c] += __shfl_down_sync(0xffffffffu, v[c], d);
+        for (int d = 16; d > 0; d >>= 1) v[c] += __shfl_xor_sync(0xffffffffu, v[c], d);
       }
-      if (lane == 0) {
+      if (lane < 7u && i < t.g.numAtoms) {
+        double a = v[0];
 #pragma unroll
-        for (int c = 0; c < 7; c++) sh[threadIdx.x >> 5][c] = v[c];
+        for (int c = 1; c < 7; c++) a = lane == (uint32_t)c ? v[c] : a;
+        if (a != 0.0) atomicAdd(grad_atoms + (t.atom_off + i) * 7u + lane, a);
       }
-      __syncthreads();
-      if (threadIdx.x < 7u && i < t.g.numAtoms) {
-        double a = 0.0;
-        for (int k = 0; k < kDiffBlock / 32; k++) a += sh[k][threadIdx.x];
-        if (a != 0.0) atomicAdd(grad_atoms + (t.atom_off + i) * 7u + threadIdx.x, a);
-      }
-      __syncthreads();
     }
+    __syncthreads();
   }
 }
 
