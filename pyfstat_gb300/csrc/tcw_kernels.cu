@@ -465,7 +465,7 @@ __device__ void exp_tile(const TemplateDev &t, const WorkItem &w, const float *_
     return;
   }
   const uint32_t *a8u = reinterpret_cast<const uint32_t *>(a8);
-  ExpColumn<kPrec == kPrecFF_F64Det> C;
+  ExpColumn<kPrec == kPrecFF_F64Det, true> C;
   C.init(t.g, tau);
   for (uint32_t ce = me; ce > mb;) {
     const uint32_t cb = ce - mb > kExpRowTab ? ce - kExpRowTab : mb;

@@ -109,7 +109,7 @@ int hc_exp_map(const float *atoms, uint32_t n, uint32_t TAtom, uint32_t t0_data,
       bool reg = comp == 1;
       for (uint32_t m = mb; reg && m < me; m++) reg = exp_row_regular(t0s[m], taus[k], g);
       if (reg) {
-        ExpColumn<false> C;
+        ExpColumn<false, true> C;
         C.init(g, taus[k]);
         for (uint32_t m = me; m-- > mb;) {
           ExpRow e;
