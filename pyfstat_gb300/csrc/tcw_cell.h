@@ -933,6 +933,38 @@ TCW_HD FF2 ff2_sub_scaled_x_fast(FF2 W, F2 ph, F2 nph, F2 pl, F2 x) {
   return FF2{s, sub2(add2(e, W.l), ae)};
 }
 
+// Exact Fast2Sum entries for A, B and C: Fast2Sum is exact when its first
+// operand is the larger in magnitude, so ordering the two operands first
+// makes it an error-free sum with the same result as TwoSum (bit for bit),
+// in three FMA-pipe operations plus min / max or compare / select on the
+// ALU pipe instead of six FMA-pipe operations.  For the (A,B) pair both
+// terms are non-negative (a2, b2 >= 0, and the decayed window sum of
+// non-negative terms), so max / min order them by magnitude.
+TCW_HD FF2 ff2_axpy_nonneg(F2 x, F2 rh, F2 nrh, F2 rl, FF2 E) {
+  const F2 q = mul2(nrh, E.h);        // -p, p = fl(r.h E.h)
+  F2 pe = fma2(rh, E.h, q);           // exact product error
+  pe = fma2(rh, E.l, pe);
+  pe = fma2(rl, E.h, pe);
+  const F2 a{fmaxf(-q.x, x.x), fmaxf(-q.y, x.y)};
+  const F2 b{fminf(-q.x, x.x), fminf(-q.y, x.y)};
+  const F2 s = add2(a, b);
+  const F2 e = sub2(b, sub2(s, a));   // exact: a is the larger
+  return FF2{s, add2(e, pe)};
+}
+
+// ff_axpy with the operands of the sum ordered by magnitude (C is signed).
+TCW_HD FF ff_axpy_ord(float x, FF r, FF E) {
+  const float p = fmul(r.h, E.h);
+  float pe = ffma(r.h, E.h, -p);
+  pe = ffma(r.h, E.l, pe);
+  pe = ffma(r.l, E.h, pe);
+  const bool pbig = fabsf(p) >= fabsf(x);
+  const float a = pbig ? p : x, b = pbig ? x : p;
+  const float s = fadd(a, b);
+  const float e = fsub(b, fsub(s, a));
+  return FF{s, fadd(e, pe)};
+}
+
 // The scalar form of ff2_sub_scaled_x (W - p*x for the C channel).
 TCW_HD FF ff_sub_scaled_x1(FF W, FF p, float x) {
   const float a = fmul(p.h, x);
@@ -952,9 +984,11 @@ TCW_HD FF ff_sub_scaled_x1(FF W, FF p, float x) {
 //     multiplication when the exponent moves by one);
 //   * an atom entering at the bottom is added by W = x + r W.
 // Every step is a double-word operation with an exact product error and an
-// error-free sum (TwoSum; Fast2Sum where ff2_axpy_fast says it is exact or
-// harmless), so W stays within a few eps^2 of the exact window sum of the
-// recurrence's weights.  If the next window is not reachable that way (it
+// error-free sum (Fast2Sum with the operands ordered by magnitude for A, B
+// and C on entry, TwoSum for C on removal, plain Fast2Sum where
+// ff2_axpy_fast says it is exact or harmless), so W stays within a few
+// eps^2 of the exact window sum of the recurrence's weights.  If the next
+// window is not reachable that way (it
 // lies above wlo or wtop, only with u32 wrap-around in the grid, or it does
 // not overlap the current one), W restarts empty at the new window's top.
 template <bool kFp64Det, class Sink>
@@ -1019,8 +1053,8 @@ TCW_HD void exp_column2(const float *__restrict__ atoms8, const Geom &g,
       F2 x[4];
       TCW_DCHECK(wlo < g.numAtoms);
       load_row8(atoms8 + (size_t)wlo * 8u, x);
-      W0 = ff2_axpy(x[0], k2.rh[0], k2.nrh[0], k2.rl[0], W0);
-      Wc = ff_axpy(x[1].x, k.r2, Wc);
+      W0 = ff2_axpy_nonneg(x[0], k2.rh[0], k2.nrh[0], k2.rl[0], W0);
+      Wc = ff_axpy_ord(x[1].x, k.r2, Wc);
       W2 = ff2_axpy_fast(x[2], k2.rh[1], k2.nrh[1], k2.rl[1], W2);
       W3 = ff2_axpy_fast(x[3], k2.rh[1], k2.nrh[1], k2.rl[1], W3);
       if (x[0].x != 0.0f || x[0].y != 0.0f) nz = wlo;
@@ -1187,22 +1221,40 @@ struct ExpColumn {
         W3 = ff2_sub_scaled_x(W3, ph1, nph1, pl1, x[3]);
       }
     }
-    while (wlo > lo) {
+    // entering atoms two at a time: both rows are requested before the
+    // first step (the steps themselves are sequential)
+    while (wlo > lo + 1u) {
+      F2 x[4], y[4];
+      TCW_DCHECK(wlo - 1u < g.numAtoms);
+      load_row8(atoms8 + (size_t)(wlo - 1u) * 8u, x);
+      load_row8(atoms8 + (size_t)(wlo - 2u) * 8u, y);
+      wlo -= 2u;
+      enter(x);
+      enter(y);
+    }
+    if (wlo > lo) {
       wlo--;
       F2 x[4];
       TCW_DCHECK(wlo < g.numAtoms);
       load_row8(atoms8 + (size_t)wlo * 8u, x);
-      W0 = ff2_axpy(x[0], k2.rh[0], k2.nrh[0], k2.rl[0], W0);
-      Wc = ff_axpy(x[1].x, k.r2, Wc);
-      if (kFastSums) {
-        W2 = ff2_axpy_fast(x[2], k2.rh[1], k2.nrh[1], k2.rl[1], W2);
-        W3 = ff2_axpy_fast(x[3], k2.rh[1], k2.nrh[1], k2.rl[1], W3);
-      } else {
-        W2 = ff2_axpy(x[2], k2.rh[1], k2.nrh[1], k2.rl[1], W2);
-        W3 = ff2_axpy(x[3], k2.rh[1], k2.nrh[1], k2.rl[1], W3);
-      }
+      enter(x);
     }
     return nz < top;  // else no data in the window: zero sums, cond = inf
+  }
+
+  // W = x + r W for one entering atom row (exp_column2's steps).
+  TCW_HDM void enter(const F2 x[4]) {
+    if (kFastSums) {
+      W0 = ff2_axpy_nonneg(x[0], k2.rh[0], k2.nrh[0], k2.rl[0], W0);
+      Wc = ff_axpy_ord(x[1].x, k.r2, Wc);
+      W2 = ff2_axpy_fast(x[2], k2.rh[1], k2.nrh[1], k2.rl[1], W2);
+      W3 = ff2_axpy_fast(x[3], k2.rh[1], k2.nrh[1], k2.rl[1], W3);
+    } else {
+      W0 = ff2_axpy(x[0], k2.rh[0], k2.nrh[0], k2.rl[0], W0);
+      Wc = ff_axpy(x[1].x, k.r2, Wc);
+      W2 = ff2_axpy(x[2], k2.rh[1], k2.nrh[1], k2.rl[1], W2);
+      W3 = ff2_axpy(x[3], k2.rh[1], k2.nrh[1], k2.rl[1], W3);
+    }
   }
 
   template <class Sink>

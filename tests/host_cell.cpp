@@ -175,6 +175,24 @@ int hc_exp_real_sums(const float *atoms, uint32_t n, uint32_t TAtom, uint32_t t0
   return 0;
 }
 
+// The error-free sum forms of the exponential columns' entering step, for
+// n cases (x, E = Eh + El, r = rh + rl): out[i * 8 + ...] =
+//   0-1 ff_axpy (TwoSum), 2-3 ff_axpy_ord, 4-5 ff2_axpy_nonneg (lane 0),
+//   6-7 ff2_axpy_fast (lane 0); each as (hi, lo).
+void hc_sum_forms(const float *x, const float *Eh, const float *El, const float *rh,
+                  const float *rl, uint64_t n, float *out) {
+  for (uint64_t i = 0; i < n; i++) {
+    const FF r{rh[i], rl[i]}, E{Eh[i], El[i]};
+    const FF a = ff_axpy(x[i], r, E), b = ff_axpy_ord(x[i], r, E);
+    const F2 X{x[i], x[i]}, RH{rh[i], rh[i]}, NRH{-rh[i], -rh[i]}, RL{rl[i], rl[i]};
+    const FF2 E2{F2{Eh[i], Eh[i]}, F2{El[i], El[i]}};
+    const FF2 c = ff2_axpy_nonneg(X, RH, NRH, RL, E2), d = ff2_axpy_fast(X, RH, NRH, RL, E2);
+    float *o = out + i * 8u;
+    o[0] = a.h; o[1] = a.l; o[2] = b.h; o[3] = b.l;
+    o[4] = c.h.x; o[5] = c.l.x; o[6] = d.h.x; o[7] = d.l.x;
+  }
+}
+
 void hc_fastdiv(uint32_t d, const uint32_t *x, uint64_t n, uint32_t *q) {
   FastDiv f = make_fastdiv(d);
   for (uint64_t i = 0; i < n; i++) q[i] = fdiv(x[i], f);

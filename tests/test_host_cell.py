@@ -240,3 +240,54 @@ def test_exp_real_tau_window_sums_match_fp64(hostcell):
         nodata = ~(mask & ((A[:, 0] != 0) | (A[:, 1] != 0))[None, None, :]).any(axis=2)
         assert np.all(ok[nodata] == 0), seed
         assert np.all(ok[~nodata] == 1), seed
+
+
+def _sum_forms(hostcell, x, Eh, El, rh, rl):
+    from _helpers import P
+
+    arrs = [np.ascontiguousarray(a, np.float32) for a in (x, Eh, El, rh, rl)]
+    out = np.empty((arrs[0].size, 8), np.float32)
+    hostcell.hc_sum_forms(*[a.ctypes.data_as(P) for a in arrs], ctypes.c_uint64(arrs[0].size),
+                          out.ctypes.data_as(P))
+    return out
+
+
+def _split(v):
+    h = v.astype(np.float32)
+    return h, (v - h.astype(np.float64)).astype(np.float32)
+
+
+def test_entering_sum_forms(hostcell):
+    """The exponential columns' entering step W = x + r W: the magnitude-ordered
+    Fast2Sum forms (A, B, C) give TwoSum's double-word bit for bit, and the
+    plain Fast2Sum form (Fa, Fb) misses at most 2^-24 |x| of the exact value,
+    and nothing when the decayed sum outweighs x."""
+    from fractions import Fraction
+
+    rng = np.random.default_rng(31)
+    n = 20000
+    r = np.exp(-rng.uniform(1e-4, 3.0, n))
+    rh, rl = _split(r)
+    # window sums from much smaller to much larger than the entering term
+    mag = 10.0 ** rng.uniform(-3, 4, n)
+    Ev = mag * rng.choice([-1.0, 1.0], n) * rng.uniform(0.5, 1.0, n)
+    Eh, El = _split(Ev)
+    x = (rng.uniform(-1, 1, n) * 10.0 ** rng.uniform(-2, 1, n)).astype(np.float32)
+    out = _sum_forms(hostcell, x, Eh, El, rh, rl)
+    assert np.array_equal(out[:, 0:2].view(np.uint32), out[:, 2:4].view(np.uint32))
+    # non-negative operands (the (A,B) pair)
+    xn, En = np.abs(x), np.abs(Ev)
+    Enh, Enl = _split(En)
+    outn = _sum_forms(hostcell, xn, Enh, Enl, rh, rl)
+    assert np.array_equal(outn[:, 0:2].view(np.uint32), outn[:, 4:6].view(np.uint32))
+    # plain Fast2Sum: compare hi + lo with TwoSum's (both as exact rationals)
+    worst = 0.0
+    for i in range(0, n, 7):
+        two = Fraction(float(out[i, 0])) + Fraction(float(out[i, 1]))
+        fast = Fraction(float(out[i, 6])) + Fraction(float(out[i, 7]))
+        miss = abs(float(fast - two))
+        p = abs(float(rh[i]) * float(Eh[i]))
+        if p >= 2.0 * abs(float(x[i])):
+            assert miss == 0.0, i
+        worst = max(worst, miss / max(abs(float(x[i])), 1e-30))
+    assert worst <= 2.0 ** -24 * 1.01, worst
