@@ -83,6 +83,28 @@ struct HostSink {
   }
 };
 
+}  // extern "C"
+
+// The map kernels' row-table walk of one column chunk (exp_rows).
+template <class Sink>
+static void exp_rows_host(const float *a8, const Geom &g, const uint32_t *t0s, uint32_t mb,
+                          uint32_t me, uint32_t tau, Sink &s) {
+  ExpColumn<false, true> C;
+  C.init(g, tau);
+  for (uint32_t m = me; m-- > mb;) {
+    ExpRow e;
+    e.lo = exp_lo(t0s[m], g);
+    e.nz = 0xFFFFFFFFu;
+    if (e.lo < g.numAtoms) memcpy(&e.nz, &a8[(size_t)e.lo * 8u + 3u], sizeof(e.nz));
+    const uint32_t d = t0s[m] - g.t0_data;
+    e.a = fdiv(d, g.div);
+    e.b = d - e.a * g.TAtom;
+    C.row(a8, g, e, m, s);
+  }
+}
+
+extern "C" {
+
 // comp = 1: what the GPU runs -- atoms in rows of 8 with the first-non-zero
 //           index in slot 3 (as the repack kernel writes them), each row
 //           chunk through the row-table column (ExpColumn) when all its rows
@@ -109,18 +131,7 @@ int hc_exp_map(const float *atoms, uint32_t n, uint32_t TAtom, uint32_t t0_data,
       bool reg = comp == 1;
       for (uint32_t m = mb; reg && m < me; m++) reg = exp_row_regular(t0s[m], taus[k], g);
       if (reg) {
-        ExpColumn<false, true> C;
-        C.init(g, taus[k]);
-        for (uint32_t m = me; m-- > mb;) {
-          ExpRow e;
-          e.lo = exp_lo(t0s[m], g);
-          e.nz = 0xFFFFFFFFu;
-          if (e.lo < n) memcpy(&e.nz, &a8[(size_t)e.lo * 8u + 3u], sizeof(e.nz));
-          const uint32_t d = t0s[m] - t0_data;
-          e.a = fdiv(d, g.div);
-          e.b = d - e.a * TAtom;
-          C.row(a8, g, e, m, s);
-        }
+        exp_rows_host(a8, g, t0s, mb, me, taus[k], s);
       } else if (comp) {
         exp_column2<false>(a8, g, t0s, mb, me, taus[k], s);
       } else {
