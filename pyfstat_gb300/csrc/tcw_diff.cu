@@ -26,8 +26,10 @@
 //            map is kept) and g dF/dtau accumulates per column;
 //            pass C (same kernel): per column, atoms ascending, the
 //            transposed recurrence H(i) = r H(i-1) + sum_{lo(m)=i} G(m)
-//            - sum_{hi(m)+1=i} G(m) r^(L(m)) gives dL/dx(i) = H(i); columns
-//            are reduced across the block and added to the atom gradient.
+//            - sum_{hi(m)+1=i} G(m) r^(L(m)) in double-word FP32 gives
+//            dL/dx(i) = H(i); each warp reduces its 32 columns per atom
+//            (recursive halving over the 7 channels) and adds the sums to
+//            the FP64 atom gradient.
 // The window-sum factor e^(-k (t_lo - t0)/tau) is left out everywhere: F does
 // not depend on it, so neither do g, dF/dW (in this frame) or dF/dtau.
 //
@@ -73,24 +75,27 @@ __device__ __forceinline__ bool exp_hi_real(uint32_t t0, double tau, const Geom 
 
 // F in FP64 with the reference's conditioning test (Rect.cu:93-118).
 struct F64Cell {
-  double F, D;
+  double F, iD;  // F and 1/D
   bool ok;
 };
 
+// The conditioning test (sumAB + disc) / (sumAB - disc) < 1e4 is taken as
+// sumAB + disc < 1e4 (sumAB - disc) with sumAB - disc > 0 (no division), and
+// F = N (1/D) with the one reciprocal the derivatives reuse: FP64 divisions
+// are long sequences at GB300's FP64 rate.
 __device__ __forceinline__ F64Cell fstat64(const double W[7]) {
   const double A = W[0], B = W[1], C = W[2];
   const double sumAB = A + B, diffAB = A - B;
   const double disc = sqrt(diffAB * diffAB + 4.0 * C * C);
   const double denom = sumAB - disc;
-  const double cond = denom > 0.0 ? (sumAB + disc) / denom : INFINITY;
   F64Cell r{2.0, 0.0, false};
-  if (cond < 1e4) {
+  if (denom > 0.0 && sumAB + disc < 1e4 * denom) {
     const double D = A * B - C * C;
     if (D > 0.0) {
       const double N = B * (W[3] * W[3] + W[4] * W[4]) + A * (W[5] * W[5] + W[6] * W[6]) -
                        2.0 * C * (W[3] * W[5] + W[4] * W[6]);
-      r.F = N / D;
-      r.D = D;
+      r.iD = 1.0 / D;
+      r.F = N * r.iD;
       r.ok = true;
     }
   }
@@ -347,6 +352,14 @@ __device__ __forceinline__ FF ff_scale_dw(FF r, FF S) {
   return FF{p, pe};
 }
 __device__ __forceinline__ double dw_value(float h, float l) { return (double)h + (double)l; }
+// E + x per lane (TwoSum of the high words, x's rounding into the low word).
+__device__ __forceinline__ FF2 ff2_add_x(FF2 E, F2 x) {
+  const F2 s = add2(E.h, x);
+  const F2 bb = sub2(s, E.h);
+  const F2 e = add2(sub2(E.h, sub2(s, bb)), sub2(x, bb));
+  return FF2{s, add2(E.l, e)};
+}
+
 
 // The backward pass's column: the window sums W of ExpColumn and their
 // tau-derivative sums V_c = sum_i (i - lo) x_c(i) r_c^(i - lo) (r_c = r^2
@@ -419,8 +432,10 @@ struct ExpColumnV {
 // e^-40 when the FP32 tier-1 F (good to ~1e-5 of F) lies more than 42 below
 // Z1 (the lnBtSG term, gB != 0) and more than 40 T + 1 below (T/2) Z2 (the
 // soft-max term, gS != 0: its exponent is then below -80); such cells
-// contribute no sources.  Pass C (the transposed recurrence) runs in FP64, with the window
-// ends of regular rows from the integer split.
+// contribute no sources.  Pass C (the transposed recurrence) runs in
+// double-word FP32 (FP64 recurrences: 95 ms on the differentiation workload,
+// with a per-channel butterfly reduction 67.6 ms, double-word 45.7 ms), with
+// the window ends of regular rows from the integer split.
 __global__ void __launch_bounds__(kDiffBlock, diff_min_blocks(1))
     diff_bwd_kernel(const DiffTemplate *__restrict__ T, const DiffItem *__restrict__ items,
                     uint32_t n_items, uint32_t *__restrict__ counter,
@@ -547,7 +562,7 @@ __global__ void __launch_bounds__(kDiffBlock, diff_min_blocks(1))
                 const double F = fc.F;
                 const double g = gb * (double)exp2f((float)(F - z1) * kLog2eF) +
                                  gs * 2.0 * (double)exp2f((float)(2.0 * F / temp - z2) * kLog2eF);
-                const double A = W[0], B = W[1], Cc = W[2], iD = 1.0 / fc.D;
+                const double A = W[0], B = W[1], Cc = W[2], iD = fc.iD;
                 const double Fa2 = W[3] * W[3] + W[4] * W[4], Fb2 = W[5] * W[5] + W[6] * W[6];
                 const double re = W[3] * W[5] + W[4] * W[6];
                 double dF[7];
@@ -628,49 +643,76 @@ __global__ void __launch_bounds__(kDiffBlock, diff_min_blocks(1))
     atomicMax(&s_end, active ? row_end(t.N_t0 - 1u) : i_begin);
     __syncthreads();
     const uint32_t i_end = s_end;
-    const double rk2 = r1 * r1;
-    double H[7] = {0, 0, 0, 0, 0, 0, 0};
+    // H in double-word FP32: (A,B) and C decay with r^2, (Fa) and (Fb) with r
+    const F2 zp{0.0f, 0.0f};
+    FF2 H01{zp, zp}, H34{zp, zp}, H56{zp, zp};
+    FF H2{0.0f, 0.0f};
+    const ExpConsts &kc = CV.C.k;
+    const ExpConsts2 &kp = CV.C.k2;
     uint32_t mi = 0, mr = 0;
     uint32_t lo_next = i_begin;
     uint32_t end_r = active ? row_end(0) : 0u;
     const float *sc0 = my_scratch + threadIdx.x;
     for (uint32_t i = i_begin; i < i_end; i++) {
       if (active) {
-#pragma unroll
-        for (int c = 0; c < 7; c++) H[c] *= (c < 3 ? rk2 : r1);
+        H01 = ff2_scale_dw(kp.rh[0], kp.nrh[0], kp.rl[0], H01);
+        H2 = ff_scale_dw(kc.r2, H2);
+        H34 = ff2_scale_dw(kp.rh[1], kp.nrh[1], kp.rl[1], H34);
+        H56 = ff2_scale_dw(kp.rh[1], kp.nrh[1], kp.rl[1], H56);
         while (mi < t.N_t0 && lo_next <= i) {
           const float *scr = sc0 + (size_t)mi * kDiffSlots * kDiffBlock;
-#pragma unroll
-          for (int c = 0; c < 7; c++) H[c] += (double)scr[(size_t)c * kDiffBlock];
+          H01 = ff2_add_x(H01, F2{scr[0], scr[(size_t)1 * kDiffBlock]});
+          H2 = ff_add1(H2, scr[(size_t)2 * kDiffBlock]);
+          H34 = ff2_add_x(H34, F2{scr[(size_t)3 * kDiffBlock], scr[(size_t)4 * kDiffBlock]});
+          H56 = ff2_add_x(H56, F2{scr[(size_t)5 * kDiffBlock], scr[(size_t)6 * kDiffBlock]});
           mi++;
           if (mi < t.N_t0) lo_next = exp_lo(__ldg(t0s + mi), t.g);
         }
         while (mr < mi && end_r <= i) {
           const float *scr = sc0 + (size_t)mr * kDiffSlots * kDiffBlock;
-          const double p1 =
-              (double)scr[(size_t)7 * kDiffBlock] + (double)scr[(size_t)8 * kDiffBlock];
-          const double p2 = p1 * p1;
-#pragma unroll
-          for (int c = 0; c < 7; c++)
-            H[c] -= (double)scr[(size_t)c * kDiffBlock] * (c < 3 ? p2 : p1);
+          const FF p1{scr[(size_t)7 * kDiffBlock], scr[(size_t)8 * kDiffBlock]};
+          const FF p2 = ff_mul(p1, p1);
+          const F2 ph0{p2.h, p2.h}, pl0{p2.l, p2.l}, nph0{-p2.h, -p2.h};
+          const F2 ph1{p1.h, p1.h}, pl1{p1.l, p1.l}, nph1{-p1.h, -p1.h};
+          H01 = ff2_sub_scaled_x(H01, ph0, nph0, pl0, F2{scr[0], scr[(size_t)1 * kDiffBlock]});
+          H2 = ff_sub_scaled_x1(H2, p2, scr[(size_t)2 * kDiffBlock]);
+          H34 = ff2_sub_scaled_x(H34, ph1, nph1, pl1,
+                                 F2{scr[(size_t)3 * kDiffBlock], scr[(size_t)4 * kDiffBlock]});
+          H56 = ff2_sub_scaled_x(H56, ph1, nph1, pl1,
+                                 F2{scr[(size_t)5 * kDiffBlock], scr[(size_t)6 * kDiffBlock]});
           mr++;
           if (mr < t.N_t0) end_r = row_end(mr);
         }
       }
-      // reduce the warp's columns' contributions to atom i; each warp adds its
-      // own (no block barrier per atom)
-      double v[7];
+      // reduce the warp's columns' contributions to atom i (each warp adds its
+      // own: no block barrier per atom) by recursive halving over 8 channel
+      // slots in double-word arithmetic: at each step a lane keeps half of its
+      // slots, sends the other half to its partner and adds what it receives
+      // (9 double-word additions per lane); lane L ends with channel
+      // (L >> 2) & 7 summed over the warp
+      const bool u16 = (lane & 16u) != 0u, u8 = (lane & 8u) != 0u, u4 = (lane & 4u) != 0u;
+      const FF zf{0.0f, 0.0f};
+      const FF slot[8] = {active ? FF{H01.h.x, H01.l.x} : zf, active ? FF{H01.h.y, H01.l.y} : zf,
+                          active ? H2 : zf,                    active ? FF{H34.h.x, H34.l.x} : zf,
+                          active ? FF{H34.h.y, H34.l.y} : zf, active ? FF{H56.h.x, H56.l.x} : zf,
+                          active ? FF{H56.h.y, H56.l.y} : zf, zf};
+      auto xch = [&](FF send, int d) {
+        return FF{__shfl_xor_sync(0xffffffffu, send.h, d), __shfl_xor_sync(0xffffffffu, send.l, d)};
+      };
+      FF k4[4], k2[2];
 #pragma unroll
-      for (int c = 0; c < 7; c++) {
-        v[c] = active ? H[c] : 0.0;
+      for (int j = 0; j < 4; j++)
+        k4[j] = ff_add_dw(u16 ? slot[4 + j] : slot[j], xch(u16 ? slot[j] : slot[4 + j], 16));
 #pragma unroll
-        for (int d = 16; d > 0; d >>= 1) v[c] += __shfl_xor_sync(0xffffffffu, v[c], d);
-      }
-      if (lane < 7u && i < t.g.numAtoms) {
-        double a = v[0];
-#pragma unroll
-        for (int c = 1; c < 7; c++) a = lane == (uint32_t)c ? v[c] : a;
-        if (a != 0.0) atomicAdd(grad_atoms + (t.atom_off + i) * 7u + lane, a);
+      for (int j = 0; j < 2; j++)
+        k2[j] = ff_add_dw(u8 ? k4[2 + j] : k4[j], xch(u8 ? k4[j] : k4[2 + j], 8));
+      FF v = ff_add_dw(u4 ? k2[1] : k2[0], xch(u4 ? k2[0] : k2[1], 4));
+      v = ff_add_dw(v, xch(v, 2));
+      v = ff_add_dw(v, xch(v, 1));
+      const uint32_t ch = (lane >> 2) & 7u;
+      if ((lane & 3u) == 0u && ch < 7u && i < t.g.numAtoms) {
+        const double a = (double)v.h + (double)v.l;
+        if (a != 0.0) atomicAdd(grad_atoms + (t.atom_off + i) * 7u + ch, a);
       }
     }
     __syncthreads();
@@ -752,7 +794,7 @@ __global__ void __launch_bounds__(kDiffBlock, diff_min_blocks(kPass))
           const double g = gb * (double)exp2f((float)(F - z1) * kLog2eF) +
                            gs * 2.0 * (double)exp2f((float)(2.0 * F / temp - z2) * kLog2eF);
           if (g == 0.0) continue;
-          const double A = S[0], B = S[1], C = S[2], iD = 1.0 / fc.D;
+          const double A = S[0], B = S[1], C = S[2], iD = fc.iD;
           const double Fa2 = S[3] * S[3] + S[4] * S[4], Fb2 = S[5] * S[5] + S[6] * S[6];
           const double re = S[3] * S[5] + S[4] * S[6];
           double G[7];
