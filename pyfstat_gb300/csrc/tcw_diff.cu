@@ -13,9 +13,10 @@
 // needs F to ~1e-9 of its value.  The exponential windows' sums slide down
 // each tau column in double-word FP32 (ExpColumn, the map kernels'
 // arithmetic, ~1e-14 of the sums' magnitude) rather than in FP64, whose rate
-// on GB300 is 1/70 of FP32; F, its derivatives and the log-sum-exps are FP64
-// for the cells that carry weight (an FP32 tier-1 F far enough below the
-// maximum or the normaliser skips a cell, whose weight is then below e^-40):
+// on GB300 is 1/70 of FP32; for the cells that carry weight (an FP32 tier-1
+// F far enough below the maximum or the normaliser skips a cell, whose
+// weight is then below e^-40) the forward forms F and the log-sum-exps in
+// FP64, the backward F, dF/dW and the sources in double-word FP32:
 //
 //   diff_fwd_kernel  per tau column, rows descending: double-word window
 //            sums, FP64 log-sum-exps of F and 2F/T -> per-tile partials ->
@@ -351,7 +352,67 @@ __device__ __forceinline__ FF ff_scale_dw(FF r, FF S) {
   pe = ffma(r.l, S.h, pe);
   return FF{p, pe};
 }
-__device__ __forceinline__ double dw_value(float h, float l) { return (double)h + (double)l; }
+// Double-word arithmetic on FF (hi + lo FP32 pairs, ~2^-44 relative per
+// operation) for the adjoint's per-cell values.
+__device__ __forceinline__ FF dw_norm(float s, float e) {
+  const float h = fadd(s, e);
+  return FF{h, fsub(e, fsub(h, s))};
+}
+__device__ __forceinline__ FF dw_add(FF a, FF b) {
+  float s, e;
+  two_sum(a.h, b.h, s, e);
+  return dw_norm(s, fadd(e, fadd(a.l, b.l)));
+}
+__device__ __forceinline__ FF dw_sub(FF a, FF b) { return dw_add(a, FF{-b.h, -b.l}); }
+__device__ __forceinline__ FF dw_mulf(FF a, float b) {
+  const float p = fmul(a.h, b);
+  float e = ffma(a.h, b, -p);
+  e = ffma(a.l, b, e);
+  return dw_norm(p, e);
+}
+__device__ __forceinline__ FF dw_twice(FF a) { return FF{2.0f * a.h, 2.0f * a.l}; }
+__device__ __forceinline__ FF dw_from(double x) {
+  const float h = (float)x;
+  return FF{h, (float)(x - (double)h)};
+}
+
+// F of a cell from its double-word window sums, in double-word arithmetic:
+// D = AB - C^2 from exact products of the high words, the conditioning test
+// cond < 1e4 as 1e4 S^2 < (1 + 1e4)^2 D (S = A + B), G = B Fa - C Fb and
+// F = (|G|^2 + D |Fb|^2) / (B D).
+struct DwCell {
+  FF F, iD, Gre, Gim, Fb2;
+  bool ok;
+};
+__device__ __forceinline__ DwCell dw_fstat(FF A, FF B, FF C, FF Far, FF Fai, FF Fbr, FF Fbi) {
+  DwCell r;
+  const float p = fmul(A.h, B.h), pe = ffma(A.h, B.h, -p);
+  const float q = fmul(C.h, C.h), qe = ffma(C.h, C.h, -q);
+  float s, se;
+  two_sum(p, -q, s, se);
+  float corr = fadd(se, fsub(pe, qe));
+  corr = ffma(A.h, B.l, corr);
+  corr = ffma(A.l, B.h, corr);
+  corr = ffma(-2.0f * C.h, C.l, corr);
+  corr = ffma(A.l, B.l, corr);
+  corr = ffma(-C.l, C.l, corr);
+  const FF D = dw_norm(s, corr);
+  const FF S = dw_add(A, B);
+  const FF lhs = dw_mulf(ff_mul(S, S), 1.0e4f);
+  const FF rhs = ff_mul(D, FF{100020000.0f, 1.0f});  // (1 + 1e4)^2
+  const FF dd = dw_sub(rhs, lhs);
+  r.ok = D.h > 0.0f && S.h > 0.0f && dd.h > 0.0f;
+  r.Gre = dw_sub(ff_mul(B, Far), ff_mul(C, Fbr));
+  r.Gim = dw_sub(ff_mul(B, Fai), ff_mul(C, Fbi));
+  r.Fb2 = dw_add(ff_mul(Fbr, Fbr), ff_mul(Fbi, Fbi));
+  const FF G2 = dw_add(ff_mul(r.Gre, r.Gre), ff_mul(r.Gim, r.Gim));
+  const FF num = dw_add(G2, ff_mul(D, r.Fb2));
+  r.iD = r.ok ? ff_recip(D) : FF{0.0f, 0.0f};
+  const FF iB = r.ok ? ff_recip(B) : FF{0.0f, 0.0f};
+  r.F = ff_mul(ff_mul(num, r.iD), iB);
+  return r;
+}
+
 // E + x per lane (TwoSum of the high words, x's rounding into the low word).
 __device__ __forceinline__ FF2 ff2_add_x(FF2 E, F2 x) {
   const F2 s = add2(E.h, x);
@@ -426,8 +487,8 @@ struct ExpColumnV {
 
 // Backward pass of exponential windows.  Pass B slides W and V down each
 // tau column in double-word FP32 (ExpColumnV) with the per-row quantities
-// tabulated per warp; a cell gets FP64 F, dF/dW and its adjoint sources only
-// when it carries weight.  Its weight g = gB e^(F - Z1) + 2 gS e^(2F/T - Z2)
+// tabulated per warp; a cell gets F, dF/dW and its adjoint sources (in
+// double-word arithmetic, dw_fstat) only when it carries weight.  Its weight g = gB e^(F - Z1) + 2 gS e^(2F/T - Z2)
 // (Z1 = logsumexp F, Z2 = logsumexp 2F/T, from the forward outputs) is below
 // e^-40 when the FP32 tier-1 F (good to ~1e-5 of F) lies more than 42 below
 // Z1 (the lnBtSG term, gB != 0) and more than 40 T + 1 below (T/2) Z2 (the
@@ -471,6 +532,9 @@ __global__ void __launch_bounds__(kDiffBlock, diff_min_blocks(1))
     const double z1 = lnZ1[w.tmpl] - log(70.0 / ((double)t.N_t0 * (double)t.N_tau));
     const double z2 = lnZ2[w.tmpl] / temp;
     const double gb = gB[w.tmpl], gs = gS[w.tmpl];
+    const FF z1w = dw_from(z1), z2w = dw_from(z2), twoT = dw_from(2.0 / temp);
+    const float gbf = (float)gb, gsf = (float)gs;
+    FF dtw{0.0f, 0.0f};
     // a tier-1 F below `skip` carries no weight in either sum
     const double sk1 = gb != 0.0 ? z1 - 42.0 : INFINITY;
     const double sk2 = gs != 0.0 ? 0.5 * temp * (z2 - 80.0) - 1.0 : INFINITY;
@@ -519,7 +583,7 @@ __global__ void __launch_bounds__(kDiffBlock, diff_min_blocks(1))
               data = CV.slide(a8, t.g, e.lo, top, e.nz);
             }
           }
-          double G[7] = {0, 0, 0, 0, 0, 0, 0};
+          float Gf[7] = {0, 0, 0, 0, 0, 0, 0};
           float p1h = 0.0f, p1l = 0.0f;
           if (data) {
             // r^L, L = top - lo, for the removal in the transposed recurrence
@@ -541,42 +605,36 @@ __global__ void __launch_bounds__(kDiffBlock, diff_min_blocks(1))
             const float sc = fadd(C.Wc.h, C.Wc.l);
             const bool t1 = fstat_fast_sums(s0.x, s0.y, sc, s2v.x, s2v.y, s3.x, s3.y, F32);
             if (!(t1 && F32 < skip)) {
-              double W[7];
-              W[0] = dw_value(C.W0.h.x, C.W0.l.x);
-              W[1] = dw_value(C.W0.h.y, C.W0.l.y);
-              W[2] = dw_value(C.Wc.h, C.Wc.l);
-              W[3] = dw_value(C.W2.h.x, C.W2.l.x);
-              W[4] = dw_value(C.W2.h.y, C.W2.l.y);
-              W[5] = dw_value(C.W3.h.x, C.W3.l.x);
-              W[6] = dw_value(C.W3.h.y, C.W3.l.y);
-              const F64Cell fc = fstat64(W);
+              const FF A{C.W0.h.x, C.W0.l.x}, B{C.W0.h.y, C.W0.l.y}, Cc = C.Wc;
+              const FF Far{C.W2.h.x, C.W2.l.x}, Fai{C.W2.h.y, C.W2.l.y};
+              const FF Fbr{C.W3.h.x, C.W3.l.x}, Fbi{C.W3.h.y, C.W3.l.y};
+              const DwCell fc = dw_fstat(A, B, Cc, Far, Fai, Fbr, Fbi);
               if (fc.ok) {
-                double V[7];
-                V[0] = dw_value(CV.V0.h.x, CV.V0.l.x);
-                V[1] = dw_value(CV.V0.h.y, CV.V0.l.y);
-                V[2] = dw_value(CV.Vc.h, CV.Vc.l);
-                V[3] = dw_value(CV.V2.h.x, CV.V2.l.x);
-                V[4] = dw_value(CV.V2.h.y, CV.V2.l.y);
-                V[5] = dw_value(CV.V3.h.x, CV.V3.l.x);
-                V[6] = dw_value(CV.V3.h.y, CV.V3.l.y);
-                const double F = fc.F;
-                const double g = gb * (double)exp2f((float)(F - z1) * kLog2eF) +
-                                 gs * 2.0 * (double)exp2f((float)(2.0 * F / temp - z2) * kLog2eF);
-                const double A = W[0], B = W[1], Cc = W[2], iD = fc.iD;
-                const double Fa2 = W[3] * W[3] + W[4] * W[4], Fb2 = W[5] * W[5] + W[6] * W[6];
-                const double re = W[3] * W[5] + W[4] * W[6];
-                double dF[7];
-                dF[0] = (Fb2 - F * B) * iD;
-                dF[1] = (Fa2 - F * A) * iD;
-                dF[2] = (2.0 * F * Cc - 2.0 * re) * iD;
-                dF[3] = 2.0 * (B * W[3] - Cc * W[5]) * iD;
-                dF[4] = 2.0 * (B * W[4] - Cc * W[6]) * iD;
-                dF[5] = 2.0 * (A * W[5] - Cc * W[3]) * iD;
-                dF[6] = 2.0 * (A * W[6] - Cc * W[4]) * iD;
+                const FF F = fc.F;
+                // exponents of the weights from double-word differences
+                const FF d1 = dw_sub(F, z1w);
+                const FF d2 = dw_sub(ff_mul(F, twoT), z2w);
+                const float g = gbf * exp2f(fadd(d1.h, d1.l) * kLog2eF) +
+                                gsf * 2.0f * exp2f(fadd(d2.h, d2.l) * kLog2eF);
+                const FF Fa2 = dw_add(ff_mul(Far, Far), ff_mul(Fai, Fai));
+                const FF re = dw_add(ff_mul(Far, Fbr), ff_mul(Fai, Fbi));
+                FF dF[7];
+                dF[0] = ff_mul(dw_sub(fc.Fb2, ff_mul(F, B)), fc.iD);
+                dF[1] = ff_mul(dw_sub(Fa2, ff_mul(F, A)), fc.iD);
+                dF[2] = dw_twice(ff_mul(dw_sub(ff_mul(F, Cc), re), fc.iD));
+                dF[3] = dw_twice(ff_mul(fc.Gre, fc.iD));
+                dF[4] = dw_twice(ff_mul(fc.Gim, fc.iD));
+                dF[5] = dw_twice(ff_mul(dw_sub(ff_mul(A, Fbr), ff_mul(Cc, Far)), fc.iD));
+                dF[6] = dw_twice(ff_mul(dw_sub(ff_mul(A, Fbi), ff_mul(Cc, Fai)), fc.iD));
+                const FF V[7] = {FF{CV.V0.h.x, CV.V0.l.x}, FF{CV.V0.h.y, CV.V0.l.y}, CV.Vc,
+                                 FF{CV.V2.h.x, CV.V2.l.x}, FF{CV.V2.h.y, CV.V2.l.y},
+                                 FF{CV.V3.h.x, CV.V3.l.x}, FF{CV.V3.h.y, CV.V3.l.y}};
 #pragma unroll
                 for (int c = 0; c < 7; c++) {
-                  G[c] = g * dF[c];
-                  dtau += G[c] * (c < 3 ? 2.0 : 1.0) * V[c];
+                  const FF Gc = dw_mulf(dF[c], g);
+                  Gf[c] = fadd(Gc.h, Gc.l);
+                  const FF tv = ff_mul(Gc, V[c]);
+                  dtw = dw_add(dtw, c < 3 ? dw_twice(tv) : tv);
                 }
                 p1h = (float)pw64;
                 p1l = (float)(pw64 - (double)p1h);
@@ -586,7 +644,7 @@ __global__ void __launch_bounds__(kDiffBlock, diff_min_blocks(1))
           TCW_DCHECK(m < scratch_rows);
           float *scr = my_scratch + (size_t)m * kDiffSlots * kDiffBlock + threadIdx.x;
 #pragma unroll
-          for (int c = 0; c < 7; c++) scr[(size_t)c * kDiffBlock] = (float)G[c];
+          for (int c = 0; c < 7; c++) scr[(size_t)c * kDiffBlock] = Gf[c];
           scr[(size_t)7 * kDiffBlock] = p1h;
           scr[(size_t)8 * kDiffBlock] = p1l;
         }
@@ -596,6 +654,7 @@ __global__ void __launch_bounds__(kDiffBlock, diff_min_blocks(1))
 
     // ---- pass B done for this tile: tau gradient, then pass C (ascending)
     __syncthreads();  // scratch of all columns written
+    dtau = (double)dtw.h + (double)dtw.l;
     const double scale = active ? (double)t.g.TAtom / (tau * tau) * dtau : 0.0;
     const double fr = (active && t.N_tau > 1) ? (double)n / (double)(t.N_tau - 1u) : 0.0;
     double dmax = scale * fr,
