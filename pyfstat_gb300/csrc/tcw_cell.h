@@ -1004,7 +1004,6 @@ TCW_HD void exp_column2(const float *__restrict__ atoms8, const Geom &g,
   uint32_t nz = 0xFFFFFFFFu;         // lowest atom >= wlo with a2 or b2 non-zero
   uint32_t Lp = 0;                   // exponent of the cached powers pw = r^Lp, p2 = r^(2 Lp)
   FF pw{1.0f, 0.0f}, p2{1.0f, 0.0f};
-  F2 ph[2], nph[2], pl[2];           // p2 and pw, packed
   bool pinit = false;
   for (uint32_t mm = m_end; mm > m_begin; mm--) {
     const uint32_t m = mm - 1u;
@@ -1023,14 +1022,18 @@ TCW_HD void exp_column2(const float *__restrict__ atoms8, const Geom &g,
       W0 = W2 = W3 = FF2{z, z};
       Wc = FF{0.0f, 0.0f};
     }
-    while (wtop > top) {
+    // The atom at wtop - 1 leaves with weight r^(wtop - 1 - wlo), then the
+    // atom at wlo - 1 enters (shifting every weight by one power of r); while
+    // atoms both leave and enter, alternating the two keeps that exponent,
+    // so the cached powers need no update.
+    auto leave = [&]() {
       wtop--;
       const uint32_t e = wtop - wlo;  // weight exponent of the leaving atom
       if (e != Lp || !pinit) {
         if (pinit && e == Lp + 1u)
           pw = ff_mul(pw, k.r1);
-        else if (pinit && e + 1u == Lp && (uint64_t)g.TAtom < 60ull * tau)
-          pw = ff_mul(pw, ff_recip(k.r1));  // r^-1 rebuilt here: no register held for it
+        else if (pinit && e + 1u == Lp && k.has_inv)
+          pw = ff_mul(pw, k.r1inv);
         else
           pw = ff_pow(k.r1, e);
         Lp = e;
@@ -1047,8 +1050,8 @@ TCW_HD void exp_column2(const float *__restrict__ atoms8, const Geom &g,
       Wc = ff_sub_scaled_x1(Wc, p2, x[1].x);
       W2 = ff2_sub_scaled_x_fast(W2, ph1, nph1, pl1, x[2]);
       W3 = ff2_sub_scaled_x_fast(W3, ph1, nph1, pl1, x[3]);
-    }
-    while (wlo > lo) {
+    };
+    auto enter = [&]() {
       wlo--;
       F2 x[4];
       TCW_DCHECK(wlo < g.numAtoms);
@@ -1058,7 +1061,13 @@ TCW_HD void exp_column2(const float *__restrict__ atoms8, const Geom &g,
       W2 = ff2_axpy_fast(x[2], k2.rh[1], k2.nrh[1], k2.rl[1], W2);
       W3 = ff2_axpy_fast(x[3], k2.rh[1], k2.nrh[1], k2.rl[1], W3);
       if (x[0].x != 0.0f || x[0].y != 0.0f) nz = wlo;
+    };
+    while (wtop > top && wlo > lo) {
+      leave();
+      enter();
     }
+    while (wtop > top) leave();
+    while (wlo > lo) enter();
     if (nz > hi) {  // no data in the window: zero sums, cond = inf
       sink(m, 2.0f, false);
       continue;
@@ -1171,8 +1180,6 @@ struct ExpColumn {
     return slide(atoms8, g, e.lo, top, e.nz);
   }
 
-  // Moves the window to the atoms [lo, top) (lo < top): false when none of
-  // them holds data (nz, the first non-zero atom >= lo, is >= top).
   // An empty window whose next atoms enter below `top`.
   TCW_HDM void reset_window(uint32_t top) {
     const F2 z{0.0f, 0.0f};
@@ -1188,7 +1195,7 @@ struct ExpColumn {
       if (pinit && ex == Lp + 1u)
         pw = ff_mul(pw, k.r1);
       else if (pinit && ex + 1u == Lp && k.has_inv)
-        pw = ff_mul(pw, ff_recip(k.r1));  // r^-1 rebuilt here: no register held for it
+        pw = ff_mul(pw, k.r1inv);
       else
         pw = ff_pow(k.r1, ex);
       Lp = ex;
@@ -1197,32 +1204,48 @@ struct ExpColumn {
     }
   }
 
+  // Removes the atom at wtop - 1 (weight r^(wtop - 1 - wlo)).
+  TCW_HDM void leave(const float *__restrict__ atoms8, const Geom &g) {
+    wtop--;
+    power(wtop - wlo);  // weight exponent of the leaving atom
+    F2 x[4];
+    TCW_DCHECK(wtop < g.numAtoms);
+    load_row8(atoms8 + (size_t)wtop * 8u, x);
+    // packed copies of the powers, formed here rather than held across rows
+    const F2 ph0{p2.h, p2.h}, pl0{p2.l, p2.l}, nph0{-p2.h, -p2.h};
+    const F2 ph1{pw.h, pw.h}, pl1{pw.l, pw.l}, nph1{-pw.h, -pw.h};
+    if (kFastSums) {
+      W0 = ff2_sub_scaled_x_fast(W0, ph0, nph0, pl0, x[0]);
+      Wc = ff_sub_scaled_x1(Wc, p2, x[1].x);
+      W2 = ff2_sub_scaled_x_fast(W2, ph1, nph1, pl1, x[2]);
+      W3 = ff2_sub_scaled_x_fast(W3, ph1, nph1, pl1, x[3]);
+    } else {
+      W0 = ff2_sub_scaled_x(W0, ph0, nph0, pl0, x[0]);
+      Wc = ff_sub_scaled_x1(Wc, p2, x[1].x);
+      W2 = ff2_sub_scaled_x(W2, ph1, nph1, pl1, x[2]);
+      W3 = ff2_sub_scaled_x(W3, ph1, nph1, pl1, x[3]);
+    }
+  }
+
+  // Moves the window to the atoms [lo, top) (lo < top): false when none of
+  // them holds data (nz, the first non-zero atom >= lo, is >= top).  The
+  // steps are exp_column2's in the same order (leaving atoms alternate with
+  // entering ones while both remain, so the leaving weight's exponent stays
+  // put), hence the same bits.
   TCW_HDM bool slide(const float *__restrict__ atoms8, const Geom &g, uint32_t lo, uint32_t top,
                      uint32_t nz) {
     if (top > wtop || lo > wlo || top <= wlo) reset_window(top);
-    while (wtop > top) {
-      wtop--;
-      power(wtop - wlo);  // weight exponent of the leaving atom
-      F2 x[4];
-      TCW_DCHECK(wtop < g.numAtoms);
-      load_row8(atoms8 + (size_t)wtop * 8u, x);
-      // packed copies of the powers, formed here rather than held across rows
-      const F2 ph0{p2.h, p2.h}, pl0{p2.l, p2.l}, nph0{-p2.h, -p2.h};
-      const F2 ph1{pw.h, pw.h}, pl1{pw.l, pw.l}, nph1{-pw.h, -pw.h};
-      if (kFastSums) {
-        W0 = ff2_sub_scaled_x_fast(W0, ph0, nph0, pl0, x[0]);
-        Wc = ff_sub_scaled_x1(Wc, p2, x[1].x);
-        W2 = ff2_sub_scaled_x_fast(W2, ph1, nph1, pl1, x[2]);
-        W3 = ff2_sub_scaled_x_fast(W3, ph1, nph1, pl1, x[3]);
-      } else {
-        W0 = ff2_sub_scaled_x(W0, ph0, nph0, pl0, x[0]);
-        Wc = ff_sub_scaled_x1(Wc, p2, x[1].x);
-        W2 = ff2_sub_scaled_x(W2, ph1, nph1, pl1, x[2]);
-        W3 = ff2_sub_scaled_x(W3, ph1, nph1, pl1, x[3]);
-      }
+    while (wtop > top && wlo > lo) {
+      F2 x[4];  // the entering row, requested before the removal
+      TCW_DCHECK(wlo - 1u < g.numAtoms);
+      load_row8(atoms8 + (size_t)(wlo - 1u) * 8u, x);
+      leave(atoms8, g);
+      wlo--;
+      enter(x);
     }
-    // entering atoms two at a time: both rows are requested before the
-    // first step (the steps themselves are sequential)
+    while (wtop > top) leave(atoms8, g);
+    // the remaining entering atoms two at a time: both rows are requested
+    // before the first step (the steps themselves are sequential)
     while (wlo > lo + 1u) {
       F2 x[4], y[4];
       TCW_DCHECK(wlo - 1u < g.numAtoms);
