@@ -1169,11 +1169,17 @@ struct ExpColumn {
     pinit = false;
   }
 
+  // floor((t0 + 3 tau + TAtom/2 - t0_data) / TAtom) of row e, the window end
+  // before its clamps to [1, numAtoms]: non-decreasing in t0.
+  TCW_HDM uint32_t top_raw(const ExpRow &e) const {
+    const uint32_t v = e.b + RmT;  // as int: >= 0 iff b + R'' >= TAtom
+    return e.a + Qp1 - (v >> 31);
+  }
+
   // Moves the window to row e's: false when it holds no atom or no data
   // (F = 2), true when W0, Wc, W2, W3 hold its sums.
   TCW_HDM bool window(const float *__restrict__ atoms8, const Geom &g, const ExpRow &e) {
-    const uint32_t v = e.b + RmT;  // as int: >= 0 iff b + R'' >= TAtom
-    uint32_t top = e.a + Qp1 - (v >> 31);
+    uint32_t top = top_raw(e);
     top = top < 1u ? 1u : top;
     top = top < g.numAtoms ? top : g.numAtoms;
     if (e.lo >= top) return false;
@@ -1244,8 +1250,23 @@ struct ExpColumn {
       enter(x);
     }
     while (wtop > top) leave(atoms8, g);
-    // the remaining entering atoms two at a time: both rows are requested
-    // before the first step (the steps themselves are sequential)
+    enter_to(atoms8, g, lo);
+    return nz < top;  // else no data in the window: zero sums, cond = inf
+  }
+
+  // slide() for a window whose end is clamped at numAtoms, where no atom
+  // leaves (wtop <= numAtoms): the same steps.
+  TCW_HDM bool slide_clamped(const float *__restrict__ atoms8, const Geom &g, uint32_t lo,
+                             uint32_t nz) {
+    const uint32_t top = g.numAtoms;
+    if (top > wtop || lo > wlo || top <= wlo) reset_window(top);
+    enter_to(atoms8, g, lo);
+    return nz < top;
+  }
+
+  // The entering atoms down to lo, two at a time: both rows are requested
+  // before the first step (the steps themselves are sequential).
+  TCW_HDM void enter_to(const float *__restrict__ atoms8, const Geom &g, uint32_t lo) {
     while (wlo > lo + 1u) {
       F2 x[4], y[4];
       TCW_DCHECK(wlo - 1u < g.numAtoms);
@@ -1262,7 +1283,6 @@ struct ExpColumn {
       load_row8(atoms8 + (size_t)wlo * 8u, x);
       enter(x);
     }
-    return nz < top;  // else no data in the window: zero sums, cond = inf
   }
 
   // W = x + r W for one entering atom row (exp_column2's steps).
@@ -1287,6 +1307,39 @@ struct ExpColumn {
       sink(m, 2.0f, false);
       return;
     }
+    emit(m, sink);
+  }
+
+  // row() where the caller knows that top_raw(e) >= numAtoms (the window
+  // end is clamped at numAtoms): the same steps without the window end's
+  // arithmetic and with no atom leaving.
+  template <class Sink>
+  TCW_HDM void row_clamped(const float *__restrict__ atoms8, const Geom &g, const ExpRow &e,
+                           uint32_t m, Sink &sink) {
+    if (e.lo >= g.numAtoms || !slide_clamped(atoms8, g, e.lo, e.nz)) {
+      sink(m, 2.0f, false);
+      return;
+    }
+    emit(m, sink);
+  }
+
+  // row_clamped() for a row that follows, in the same walk, a clamped row
+  // whose window held an atom, with e.lo no larger than that row's: the
+  // window neither restarts nor loses atoms, and it holds an atom.
+  template <class Sink>
+  TCW_HDM void row_steady(const float *__restrict__ atoms8, const Geom &g, const ExpRow &e,
+                          uint32_t m, Sink &sink) {
+    enter_to(atoms8, g, e.lo);
+    if (e.nz >= g.numAtoms) {  // no data in the window: zero sums, cond = inf
+      sink(m, 2.0f, false);
+      return;
+    }
+    emit(m, sink);
+  }
+
+  // F of the current window sums (tier 1, else tier 2) to the sink.
+  template <class Sink>
+  TCW_HDM void emit(uint32_t m, Sink &sink) {
     bool ok = true;
     float F;
     const F2 s0 = add2(W0.h, W0.l), s2 = add2(W2.h, W2.l), s3 = add2(W3.h, W3.l);

@@ -197,8 +197,8 @@ struct Red {
   // with it, so only that row is kept per cell (row_to_index forms the flat
   // index once per column).
   uint32_t brow;  // row (exp columns) or column (rect rows) of the max
+  // NaN cells are skipped: they fail both comparisons and the -60 test.
   __device__ __forceinline__ void add_row_desc(float F, uint32_t m) {
-    if (F != F) return;  // NaN cells are skipped
     if (F > mx) {
       const float sc = ex2_approx((mx - F) * kLog2e);
       s *= sc;
@@ -454,8 +454,10 @@ __device__ __forceinline__ void exp_rows(const TemplateDev &t, const float *__re
   for (uint32_t ce = me; ce > mb;) {
     const uint32_t cb = ce - mb > kExpRowTab ? ce - kExpRowTab : mb;
     __syncwarp();
+    uint32_t t0min = 0xFFFFFFFFu;
     for (uint32_t r = lane; r < ce - cb; r += 32u) {
       const uint32_t t0 = __ldg(t0s + cb + r);
+      t0min = min(t0min, t0);
       ExpRow e;
       e.lo = exp_lo(t0, t.g);
       e.nz = e.lo < t.g.numAtoms ? __ldg(a8u + (size_t)e.lo * 8u + 3u) : 0xFFFFFFFFu;
@@ -465,10 +467,42 @@ __device__ __forceinline__ void exp_rows(const TemplateDev &t, const float *__re
       tab[r] = e;
     }
     __syncwarp();
+    // the window end grows with t0: if it is clamped at numAtoms for the
+    // chunk's smallest t0, it is for every row of the chunk
+    ExpRow e0;
+    const uint32_t d0 = __reduce_min_sync(0xffffffffu, t0min) - t.g.t0_data;
+    e0.a = fdiv(d0, t.g.div);
+    e0.b = d0 - e0.a * t.g.TAtom;
+    const bool clamped = __all_sync(0xffffffffu, !active || C.top_raw(e0) >= t.g.numAtoms);
+    // window starts that never grow along the walk (t0 non-decreasing in m)
+    bool mono = true;
+    for (uint32_t r = lane; r + 1u < ce - cb; r += 32u) mono = mono && tab[r].lo <= tab[r + 1u].lo;
+    mono = __all_sync(0xffffffffu, mono);
     if (active) {
-      for (uint32_t m = ce; m > cb;) {
-        m--;
-        C.row(a8, t.g, tab[m - cb], m, sink);
+      if (clamped && mono) {
+        // the rows before the first window with an atom, that row, then the
+        // steady rows (row_steady's conditions hold for all of them)
+        uint32_t m = ce;
+        while (m > cb) {
+          m--;
+          const ExpRow &e = tab[m - cb];
+          C.row_clamped(a8, t.g, e, m, sink);
+          if (e.lo < t.g.numAtoms) break;
+        }
+        while (m > cb) {
+          m--;
+          C.row_steady(a8, t.g, tab[m - cb], m, sink);
+        }
+      } else if (clamped) {
+        for (uint32_t m = ce; m > cb;) {
+          m--;
+          C.row_clamped(a8, t.g, tab[m - cb], m, sink);
+        }
+      } else {
+        for (uint32_t m = ce; m > cb;) {
+          m--;
+          C.row(a8, t.g, tab[m - cb], m, sink);
+        }
       }
     }
     ce = cb;

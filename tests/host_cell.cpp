@@ -85,21 +85,54 @@ struct HostSink {
 
 }  // extern "C"
 
-// The map kernels' row-table walk of one column chunk (exp_rows).
+// The map kernels' row-table walk of one column chunk (exp_rows): row tables
+// of 128 rows, each taking the clamped-window-end rows (row_clamped, and
+// row_steady after the first window with an atom when the window starts never
+// grow) when the window end is clamped at numAtoms for the table's smallest
+// t0.
 template <class Sink>
 static void exp_rows_host(const float *a8, const Geom &g, const uint32_t *t0s, uint32_t mb,
                           uint32_t me, uint32_t tau, Sink &s) {
   ExpColumn<false, true> C;
   C.init(g, tau);
-  for (uint32_t m = me; m-- > mb;) {
+  auto row_of = [&](uint32_t t0) {
     ExpRow e;
-    e.lo = exp_lo(t0s[m], g);
+    e.lo = exp_lo(t0, g);
     e.nz = 0xFFFFFFFFu;
     if (e.lo < g.numAtoms) memcpy(&e.nz, &a8[(size_t)e.lo * 8u + 3u], sizeof(e.nz));
-    const uint32_t d = t0s[m] - g.t0_data;
+    const uint32_t d = t0 - g.t0_data;
     e.a = fdiv(d, g.div);
     e.b = d - e.a * g.TAtom;
-    C.row(a8, g, e, m, s);
+    return e;
+  };
+  for (uint32_t ce = me; ce > mb;) {
+    const uint32_t cb = ce - mb > 128u ? ce - 128u : mb;
+    uint32_t t0min = 0xFFFFFFFFu;
+    for (uint32_t m = cb; m < ce; m++) t0min = t0s[m] < t0min ? t0s[m] : t0min;
+    const bool clamped = C.top_raw(row_of(t0min)) >= g.numAtoms;
+    bool mono = true;
+    for (uint32_t m = cb; m + 1u < ce; m++) mono = mono && row_of(t0s[m]).lo <= row_of(t0s[m + 1u]).lo;
+    if (clamped && mono) {
+      uint32_t m = ce;
+      while (m > cb) {
+        m--;
+        const ExpRow e = row_of(t0s[m]);
+        C.row_clamped(a8, g, e, m, s);
+        if (e.lo < g.numAtoms) break;
+      }
+      while (m > cb) {
+        m--;
+        C.row_steady(a8, g, row_of(t0s[m]), m, s);
+      }
+    } else {
+      for (uint32_t m = ce; m-- > cb;) {
+        if (clamped)
+          C.row_clamped(a8, g, row_of(t0s[m]), m, s);
+        else
+          C.row(a8, g, row_of(t0s[m]), m, s);
+      }
+    }
+    ce = cb;
   }
 }
 
