@@ -1131,6 +1131,8 @@ struct ExpColumn {
   uint32_t wlo, wtop, Lp;
   FF pw, p2;          // r^Lp and r^(2 Lp); their packed copies are formed per removal
   bool pinit;
+  float Fl;           // the last row's F and flag (row_clamped, row_steady)
+  bool okl;
 
   TCW_HDM void init(const Geom &g, uint32_t tau) {
     k = exp_consts(g.TAtom, tau);
@@ -1317,6 +1319,8 @@ struct ExpColumn {
   TCW_HDM void row_clamped(const float *__restrict__ atoms8, const Geom &g, const ExpRow &e,
                            uint32_t m, Sink &sink) {
     if (e.lo >= g.numAtoms || !slide_clamped(atoms8, g, e.lo, e.nz)) {
+      Fl = 2.0f;
+      okl = false;
       sink(m, 2.0f, false);
       return;
     }
@@ -1325,12 +1329,20 @@ struct ExpColumn {
 
   // row_clamped() for a row that follows, in the same walk, a clamped row
   // whose window held an atom, with e.lo no larger than that row's: the
-  // window neither restarts nor loses atoms, and it holds an atom.
+  // window neither restarts nor loses atoms, and it holds an atom.  A row
+  // whose window starts where the previous row's did (t0 closer than TAtom)
+  // has that row's window, hence its F.
   template <class Sink>
   TCW_HDM void row_steady(const float *__restrict__ atoms8, const Geom &g, const ExpRow &e,
                           uint32_t m, Sink &sink) {
+    if (e.lo == wlo) {
+      sink(m, Fl, okl);
+      return;
+    }
     enter_to(atoms8, g, e.lo);
     if (e.nz >= g.numAtoms) {  // no data in the window: zero sums, cond = inf
+      Fl = 2.0f;
+      okl = false;
       sink(m, 2.0f, false);
       return;
     }
@@ -1348,6 +1360,8 @@ struct ExpColumn {
       F = fstat_ff<kFp64Det>(FF{W0.h.x, W0.l.x}, FF{W0.h.y, W0.l.y}, Wc, FF{W2.h.x, W2.l.x},
                              FF{W2.h.y, W2.l.y}, FF{W3.h.x, W3.l.x}, FF{W3.h.y, W3.l.y}, ok);
     }
+    Fl = F;
+    okl = ok;
     sink(m, F, ok);
   }
 };

@@ -177,6 +177,7 @@ struct Red {
     mx = -INFINITY;
     bidx = INT64_MAX;
     brow = 0;
+    last = 0.0f;
     s = 0.0f;
     c = 0.0f;
     f = 0.0f;
@@ -233,9 +234,17 @@ struct Red {
       mx = F;
       brow = n;
       f = fadd(f, 1.0f);
+      last = ex2_approx(0.0f);  // what add_col_asc would add for F again
     } else {
-      f = fadd(f, ex2_approx((F - mx) * kLog2e));
+      last = ex2_approx((F - mx) * kLog2e);
+      f = fadd(f, last);
     }
+  }
+  // add_col_asc for the same F as the previous column's: the same term.
+  float last;
+  __device__ __forceinline__ void add_col_same(float F) {
+    if (F != F) return;
+    f = fadd(f, last);
   }
   __device__ __forceinline__ void fold() {
     add_term(f);
@@ -354,17 +363,24 @@ __device__ void rect_tile(const TemplateDev &t, const WorkItem &w,
     ld_row16(P + (size_t)(e_cur + 1u) * kPrefixStride, cur);
   }
   // One cell: F of column n from prefix row `a` (end ea); the next column's
-  // prefix row is loaded into `b` (end eb) while this one is computed.
+  // prefix row is loaded into `b` (end eb) while this one is computed.  A
+  // column whose window end equals the previous column's has the same
+  // window, hence the same F: it takes the previous F, and its prefix row is
+  // not loaded (the window ends of a row are clamped at the last atom once
+  // t0 + tau passes the data, and taus closer than TAtom share ends).
+  uint32_t e_prev = 0xFFFFFFFFu;  // end of the previous column (none yet)
+  float F_prev = 2.0f;
   auto cell = [&](uint32_t n, uint32_t cb, const float *a, uint32_t ea, float *b,
                   uint32_t &eb) {
     if (row_ok && n + 1u < ne) {
       eb = end_of(n + 1u < cb + 32u ? stau[n + 1u - cb] : __ldg(taus + n + 1u));
       TCW_DCHECK(eb + 1u <= t.g.numAtoms);
-      ld_row16(P + (size_t)(eb + 1u) * kPrefixStride, b);
+      if (eb != ea) ld_row16(P + (size_t)(eb + 1u) * kPrefixStride, b);
     }
-    float F = 2.0f;
+    float F = F_prev;
     if (row_ok) {
-      if (ea >= j0) {
+      if (ea != e_prev) F = 2.0f;
+      if (ea != e_prev && ea >= j0) {
         bool ok;
         if (kPrec == kPrecPlain32) {
           F = fstat_plain32(fsub(a[0], row0[0]), fsub(a[1], row0[1]), fsub(a[2], row0[2]),
@@ -380,8 +396,13 @@ __device__ void rect_tile(const TemplateDev &t, const WorkItem &w,
           F = fstat_tiered2<kPrec == kPrecFF_F64Det>(W, ok);
         }
       }
-      red.add_col_asc(F, n);
+      if (ea != e_prev)
+        red.add_col_asc(F, n);
+      else
+        red.add_col_same(F);
     }
+    e_prev = ea;
+    F_prev = F;
     if (kWrite) smw[lane * 33u + (n - cb)] = F;
   };
   for (uint32_t cb = nb; cb < ne; cb += 32u) {
