@@ -410,8 +410,33 @@ __device__ void rect_tile(const TemplateDev &t, const WorkItem &w,
     __syncwarp();
     if (cb + lane < ne) stau[lane] = __ldg(taus + cb + lane);
     __syncwarp();
-    // ping-pong between the two row buffers; `cur` holds column n on entry
+    // A chunk inside every warp row's clamped run -- the window ends of the
+    // previous column and of column cb at the last atom, the chunk's taus
+    // (and the next chunk's first) non-decreasing, t0 + tau past the u32
+    // wrap of the reference's end index and without overflow, TAtom >= 2 (so
+    // the end index's quotient never reaches 2^31) -- has the last atom as
+    // every window end, so every column repeats the previous F.
+    const uint32_t nlast = ce - cb - 1u;
+    const uint32_t tx = ce < ne ? __ldg(taus + ce) : 0u;
+    bool mono = true;
+    if (lane < nlast) mono = stau[lane] <= stau[lane + 1u];
+    if (lane == nlast && ce < ne) mono = stau[lane] <= tx;
+    const uint32_t tmax = ce < ne ? tx : stau[nlast];
+    const bool clamped_run =
+        !row_ok || (t.g.TAtom >= 2u && e_cur == t.g.numAtoms - 1u &&
+                    e_prev == t.g.numAtoms - 1u &&
+                    (uint64_t)t0 + stau[0] + t.g.half >= (uint64_t)t.g.t0_data &&
+                    (uint64_t)t0 + tmax + t.g.half - t.g.t0_data <= 0xFFFFFFFFull &&
+                    (uint64_t)t0 + tmax <= 0xFFFFFFFFull);
     uint32_t n = cb;
+    if (__all_sync(0xffffffffu, mono && clamped_run)) {
+      for (; n < ce; n++) {
+        if (row_ok) red.add_col_same(F_prev);
+        if (kWrite) smw[lane * 33u + (n - cb)] = F_prev;
+      }
+      e_cur = t.g.numAtoms - 1u;  // the end of column ce
+    }
+    // ping-pong between the two row buffers; `cur` holds column n on entry
     for (; n + 1u < ce; n += 2u) {
       uint32_t e_nxt = 0;
       cell(n, cb, cur, e_cur, nxt, e_nxt);
