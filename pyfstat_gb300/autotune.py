@@ -5,7 +5,13 @@ launches them one after the other): the rectangular kernel over
 (rows per tile, columns per tile) and the exponential kernel over (columns
 per block, rows per thread chunk).  Timing uses ``tcw_plan_run_timed`` (CUDA
 events between the kernels) on a seeded sample of the batch's templates of
-about ``budget_cells`` cells per window type, best of ``repeats`` runs.
+about ``budget_cells`` cells per window type, best of ``repeats`` runs.  The
+default budget (4e9 cells, some 15 ms of kernel time per window type) takes
+whole batches of the benchmark's size: the persistent kernels' tails weigh
+on a small sample far more than on the full batch (a 4e8-cell sample of the
+4096-template batch gives each warp about two exponential tiles) and make
+short row chunks look better than they are (19.5 ms with whole columns
+against 21.3 ms with 1024-row chunks on the full batch).
 
 Choices are cached per device name and workload signature (window mix and
 log2-bucketed mean grid sizes and atom counts) in a JSON file:
@@ -116,7 +122,7 @@ def _time_plan(handle, desc, t0s, taus, cfg, flags, d_atoms, d_res, repeats):
         plan.close()
 
 
-def tune(desc, t0s, taus, atoms, handle, flags=_lib.TCW_FLAG_LNBTSG, budget_cells=4e8,
+def tune(desc, t0s, taus, atoms, handle, flags=_lib.TCW_FLAG_LNBTSG, budget_cells=4e9,
          repeats=2, use_cache=True, verbose=False):
     """Best tile config (dict) for this batch on ``handle``'s device."""
     import torch
