@@ -257,4 +257,76 @@ void hc_exp_window(uint32_t n, uint32_t TAtom, uint32_t t0_data, const uint32_t 
   }
 }
 
+
+// The rect map kernel's walk (rect_tile) restated on the host: 32-row groups,
+// columns ascending in 32-column chunks; a column whose window end equals
+// the previous column's takes the previous F, and a chunk inside every
+// row's clamped run (the kernel's test over the group's rows) repeats it
+// for all its columns.  Gives the F map only (comp = 1 arithmetic).
+int hc_rect_walk_map(const float *atoms, uint32_t n, uint32_t TAtom, uint32_t t0_data,
+                     const uint32_t *t0s, uint32_t N_t0, const uint32_t *taus, uint32_t N_tau,
+                     float *F) {
+  Geom g = make_geom(n, TAtom, t0_data);
+  float *P = (float *)malloc(sizeof(float) * (size_t)(n + 1) * kPrefixStride);
+  if (!P) return -1;
+  hc_prefix(atoms, n, 1, P);
+  for (uint32_t mg = 0; mg < N_t0; mg += 32u) {
+    uint32_t t0[32], j0[32], ef[32], e_cur[32], e_prev[32];
+    bool wr[32], ok_row[32];
+    float F_prev[32];
+    for (uint32_t l = 0; l < 32u; l++) {
+      const uint32_t m = mg + l;
+      ok_row[l] = m < N_t0;
+      if (!ok_row[l]) continue;
+      t0[l] = t0s[m];
+      j0[l] = idx_start(t0[l], g);
+      wr[l] = rect_row_wrapped(t0[l], taus[0], g);
+      ef[l] = idx_end(t0[l] + taus[0], g);
+      e_cur[l] = rect_end(t0[l], taus[0], ef[l], wr[l], g);
+      e_prev[l] = 0xFFFFFFFFu;
+      F_prev[l] = 2.0f;
+    }
+    for (uint32_t cb = 0; cb < N_tau; cb += 32u) {
+      const uint32_t ce = cb + 32u < N_tau ? cb + 32u : N_tau;
+      bool mono = true;
+      for (uint32_t k = cb; k + 1u < ce; k++) mono = mono && taus[k] <= taus[k + 1u];
+      if (ce < N_tau) mono = mono && taus[ce - 1u] <= taus[ce];
+      const uint32_t tmax = ce < N_tau ? taus[ce] : taus[ce - 1u];
+      bool run = mono;
+      for (uint32_t l = 0; l < 32u && run; l++) {
+        if (!ok_row[l]) continue;
+        run = g.TAtom >= 2u && e_cur[l] == g.numAtoms - 1u && e_prev[l] == g.numAtoms - 1u &&
+              (uint64_t)t0[l] + taus[cb] + g.half >= (uint64_t)g.t0_data &&
+              (uint64_t)t0[l] + tmax + g.half - g.t0_data <= 0xFFFFFFFFull &&
+              (uint64_t)t0[l] + tmax <= 0xFFFFFFFFull;
+      }
+      uint32_t nc = cb;
+      if (run) {
+        for (; nc < ce; nc++)
+          for (uint32_t l = 0; l < 32u; l++)
+            if (ok_row[l]) F[(size_t)(mg + l) * N_tau + nc] = F_prev[l];
+        for (uint32_t l = 0; l < 32u; l++) e_cur[l] = g.numAtoms - 1u;
+      }
+      for (; nc < ce; nc++) {
+        for (uint32_t l = 0; l < 32u; l++) {
+          if (!ok_row[l]) continue;
+          const uint32_t ea = e_cur[l];
+          uint32_t eb = 0;
+          if (nc + 1u < N_tau) eb = rect_end(t0[l], taus[nc + 1u], ef[l], wr[l], g);
+          float Fv = F_prev[l];
+          if (ea != e_prev[l]) {
+            bool ok;
+            Fv = rect_cell<true, false>(P, P + (size_t)j0[l] * kPrefixStride, j0[l], ea, ok);
+          }
+          F[(size_t)(mg + l) * N_tau + nc] = Fv;
+          e_prev[l] = ea;
+          F_prev[l] = Fv;
+          e_cur[l] = eb;
+        }
+      }
+    }
+  }
+  free(P);
+  return 0;
+}
 }  // extern "C"

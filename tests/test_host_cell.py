@@ -30,6 +30,49 @@ def test_fastdiv_matches_integer_division(hostcell):
         assert np.array_equal(q, xs // np.uint32(d)), d
 
 
+def test_rect_walk_reuse_equals_per_cell(hostcell):
+    """The rect map kernel's walk -- a column whose window end equals the
+    previous column's reuses its F, a 32-column chunk inside every row's
+    clamped run repeats it -- gives bit-identical maps to computing every
+    cell: random gappy atoms, TAtom other than 1800, t0 grids starting
+    before the data (u32 wrap of the reference's end index), tau steps
+    below TAtom (shared ends), taus past the data (clamped runs) and
+    shuffled tau grids (no run test passes)."""
+    from _helpers import P
+
+    checked = runs = 0
+    for seed in range(40):
+        rng = np.random.default_rng(900 + seed)
+        TAtom = 1800 if seed % 3 else int(rng.integers(2, 5000))
+        t0_data, A = synth.merged_atoms(seed, int(rng.integers(5, 300)), int(rng.integers(1, 3)),
+                                        Tsft=TAtom, gap_frac=float(rng.uniform(0, 0.4)))
+        n = A.shape[0]
+        nt0, ntau = int(rng.integers(1, 100)), int(rng.integers(1, 150))
+        t0 = int(t0_data + rng.integers(-3 * TAtom if seed % 5 == 0 else 0, n * TAtom))
+        t0s = (t0 + np.arange(nt0) * int(rng.integers(1, 2 * TAtom))).astype(np.uint32)
+        step = int(rng.integers(0, 2 * TAtom)) if seed % 2 else int(rng.integers(1, TAtom // 2 + 2))
+        taus = (int(rng.integers(1, 2 * TAtom)) + np.arange(ntau) * step).astype(np.uint32)
+        if seed % 7 == 3:
+            taus = rng.permutation(taus)
+        out = []
+        for fn in ("hc_rect_walk_map", "hc_rect_map"):
+            F = np.empty((nt0, ntau), np.float32)
+            args = [A.ctypes.data_as(P), ctypes.c_uint32(n), ctypes.c_uint32(TAtom),
+                    ctypes.c_uint32(t0_data), t0s.ctypes.data_as(P), ctypes.c_uint32(nt0),
+                    taus.ctypes.data_as(P), ctypes.c_uint32(ntau)]
+            if fn == "hc_rect_map":
+                ok = np.empty((nt0, ntau), np.uint8)
+                getattr(hostcell, fn)(*args, ctypes.c_int(1), F.ctypes.data_as(P),
+                                      ok.ctypes.data_as(P))
+            else:
+                getattr(hostcell, fn)(*args, F.ctypes.data_as(P))
+            out.append(F)
+        assert np.array_equal(out[0].view(np.uint32), out[1].view(np.uint32)), seed
+        checked += out[0].size
+        runs += int(np.sum(out[1][:, 1:] == out[1][:, :-1]))
+    assert checked > 100000 and runs > 10000
+
+
 def test_exp_window_bounds_match_reference_loop(hostcell, oracle):
     """[lo, hi] = atoms with t0 <= t_i <= t0 + 3 tau inside [i_t0, i_t1] (Exp.cu:80-90)."""
     rng = np.random.default_rng(1)
