@@ -1349,6 +1349,19 @@ struct ExpColumn {
     emit(m, sink);
   }
 
+  // row_steady() for a row that follows, in the same walk, a steady row whose
+  // window held data: its window (starting no higher) holds data too.
+  template <class Sink>
+  TCW_HDM void row_steady_data(const float *__restrict__ atoms8, const Geom &g, const ExpRow &e,
+                               uint32_t m, Sink &sink) {
+    if (e.lo == wlo) {
+      sink(m, Fl, okl);
+      return;
+    }
+    enter_to(atoms8, g, e.lo);
+    emit(m, sink);
+  }
+
   // F of the current window sums (tier 1, else tier 2) to the sink.
   template <class Sink>
   TCW_HDM void emit(uint32_t m, Sink &sink) {

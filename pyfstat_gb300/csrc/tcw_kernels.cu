@@ -200,17 +200,18 @@ struct Red {
   uint32_t brow;  // row (exp columns) or column (rect rows) of the max
   // NaN cells are skipped: they fail both comparisons and the -60 test.
   __device__ __forceinline__ void add_row_desc(float F, uint32_t m) {
-    if (F > mx) {
-      const float sc = ex2_approx((mx - F) * kLog2e);
-      s *= sc;
-      c *= sc;
-      mx = F;
+    if (F >= mx) {  // one test for the common F < mx
       brow = m;
-      add_term(1.0f);
-    } else {
-      if (F == mx) brow = m;
-      add_small((F - mx) * kLog2e);
+      if (F > mx) {
+        const float sc = ex2_approx((mx - F) * kLog2e);
+        s *= sc;
+        c *= sc;
+        mx = F;
+        add_term(1.0f);
+        return;
+      }
     }
+    add_small((F - mx) * kLog2e);
   }
   __device__ __forceinline__ void row_to_index(uint32_t N_tau, uint32_t n) {
     if (mx != -INFINITY) bidx = (int64_t)brow * N_tau + n;
@@ -527,7 +528,8 @@ __device__ __forceinline__ void exp_rows(const TemplateDev &t, const float *__re
     if (active) {
       if (clamped && mono) {
         // the rows before the first window with an atom, that row, then the
-        // steady rows (row_steady's conditions hold for all of them)
+        // steady rows (row_steady's conditions hold for all of them; after
+        // the first window with data, row_steady_data's too)
         uint32_t m = ce;
         while (m > cb) {
           m--;
@@ -535,9 +537,16 @@ __device__ __forceinline__ void exp_rows(const TemplateDev &t, const float *__re
           C.row_clamped(a8, t.g, e, m, sink);
           if (e.lo < t.g.numAtoms) break;
         }
+        // once a window holds data, every later (lower-starting) one does
         while (m > cb) {
           m--;
-          C.row_steady(a8, t.g, tab[m - cb], m, sink);
+          const ExpRow &e = tab[m - cb];
+          C.row_steady(a8, t.g, e, m, sink);
+          if (e.nz < t.g.numAtoms) break;
+        }
+        while (m > cb) {
+          m--;
+          C.row_steady_data(a8, t.g, tab[m - cb], m, sink);
         }
       } else if (clamped) {
         for (uint32_t m = ce; m > cb;) {

@@ -122,7 +122,13 @@ static void exp_rows_host(const float *a8, const Geom &g, const uint32_t *t0s, u
       }
       while (m > cb) {
         m--;
-        C.row_steady(a8, g, row_of(t0s[m]), m, s);
+        const ExpRow e = row_of(t0s[m]);
+        C.row_steady(a8, g, e, m, s);
+        if (e.nz < g.numAtoms) break;
+      }
+      while (m > cb) {
+        m--;
+        C.row_steady_data(a8, g, row_of(t0s[m]), m, s);
       }
     } else {
       for (uint32_t m = ce; m-- > cb;) {
