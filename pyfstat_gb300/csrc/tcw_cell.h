@@ -461,15 +461,19 @@ TCW_HD float fstat_ff(FF A, FF B, FF C, FF Far, FF Fai, FF Fbr, FF Fbi, bool &ok
 // The selection needs no square root: with S = A + B > 0 and D > 0 the
 // eigenvalues of [[A, C], [C, B]] are (S +- sqrt(S^2 - 4D))/2, and
 // cond < K  <=>  sqrt(S^2 - 4D) (1 + K) < S (K - 1)  <=>  K S^2 < (1 + K)^2 D.
-// A cell with D <= 0 (or a NaN) fails the test and goes to tier 2.
+// A cell with D <= 0 (or a NaN) fails the test and goes to tier 2.  With
+// K = 32 a power of two the test is evaluated as S^2 < ((1 + K)^2 / K) D
+// (1089 / 32 = 34.03125 exactly): scaling by K commutes with the roundings
+// (away from overflow and underflow), so it decides as
+// fl(fl(K S) S) < fl((1 + K)^2 D) with one multiplication fewer.
 constexpr float kFastCond = 32.0f;
-constexpr float kFastCondRhs = (1.0f + kFastCond) * (1.0f + kFastCond);
+constexpr float kFastCondRhs = (1.0f + kFastCond) * (1.0f + kFastCond) / kFastCond;
 
 TCW_HD bool fstat_fast_sums(float A, float B, float C, float Far, float Fai, float Fbr,
                             float Fbi, float &F) {
   const float D = ffma(A, B, -fmul(C, C));
   const float S = fadd(A, B);
-  if (!(fmul(fmul(kFastCond, S), S) < fmul(kFastCondRhs, D))) return false;
+  if (!(fmul(S, S) < fmul(kFastCondRhs, D))) return false;
   const float Gre = ffma(B, Far, -fmul(C, Fbr));
   const float Gim = ffma(B, Fai, -fmul(C, Fbi));
   const float num = ffma(D, ffma(Fbr, Fbr, fmul(Fbi, Fbi)), ffma(Gre, Gre, fmul(Gim, Gim)));
