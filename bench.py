@@ -468,6 +468,38 @@ def profile_figure(kernel, key):
     return None
 
 
+def rect_reused_fraction(desc, t0s, taus, n_sample=64, seed=99):
+    """Fraction of the rect cells whose window end equals the previous
+    column's in the row (the rect map kernel reuses their F instead of
+    evaluating it), on a seeded sample of the batch's rect templates; the
+    end index is the kernel's (rect_end: the reference's u32 arithmetic,
+    clamps, and the running maximum of wrapped rows)."""
+    idx = np.flatnonzero(desc["window"] == 1)
+    if idx.size == 0:
+        return None
+    idx = np.random.default_rng(seed).permutation(idx)[:n_sample]
+    same = total = 0
+    for k in idx:
+        d = desc[k]
+        T, t0d, N = int(d["TAtom"]), int(d["t0_data"]), int(d["numAtoms"])
+        g0 = t0s[int(d["t0_offset"]):int(d["t0_offset"]) + int(d["N_t0"])].astype(np.uint64)
+        tu = taus[int(d["tau_offset"]):int(d["tau_offset"]) + int(d["N_tau"])].astype(np.uint64)
+        m32 = np.uint64(0xFFFFFFFF)
+
+        def end(t1):
+            q = (((t1 - np.uint64(t0d) + np.uint64(T // 2)) & m32) // np.uint64(T) - 1) & m32
+            i = q.astype(np.int64)
+            i = np.where(i >= 2 ** 31, i - 2 ** 32, i)  # the cast to int
+            return np.clip(i, 0, N - 1)
+
+        e = end((g0[:, None] + tu[None, :]) & m32)
+        wr = g0 + tu[0] + np.uint64(T // 2) < np.uint64(t0d)
+        e = np.where(wr[:, None], np.maximum(e, end((g0 + tu[0]) & m32)[:, None]), e)
+        same += int(np.sum(e[:, 1:] == e[:, :-1]))
+        total += e.size
+    return same / total
+
+
 def roofline_block(batch, rect_ms, exp_ms, prefix_ms, fin_ms, peaks, clk, n_sms):
     """Roofline of the dominant map kernel: cells/s against the minimum over
     {FP32, MUFU, FP64, HBM} of measured peak / per-cell algorithmic demand,
@@ -519,6 +551,14 @@ def roofline_block(batch, rect_ms, exp_ms, prefix_ms, fin_ms, peaks, clk, n_sms)
                               "mul + fma, lnBtSG as add) x cells/s; peak = measured FP64 FMA "
                               "rate with an FMA counted as 2 flops")
             k["frac_fp64_flops"] = cps * FP64_FLOPS_PER_CELL / (peaks["fp64_tflops"] * 1e12)
+        if w == 1:
+            reused = rect_reused_fraction(desc, batch.t0s, batch.taus)
+            if reused is not None:
+                k["cells_reusing_F"] = reused
+                k["reuse_note"] = ("a cell whose window end equals its left neighbour's has "
+                                   "that cell's window and F, which the kernel reuses; the "
+                                   "per-cell FP64 count assumes every cell forms D, so frac "
+                                   "can exceed 1 (sampled on 64 rect templates)")
         current = profile_is_current(name)
         k["profile_source_current"] = current
         ipc = profile_figure(name, "warp_instructions_per_cell")
