@@ -4,8 +4,9 @@ Workload (N=1): 4096 templates, SFT counts uniform in 200..4000 with 0-30 %
 of SFTs dropped as gaps, half rectangular and half exponential windows,
 (t0, tau) grid sizes uniform in 256..2048 per axis -- about 5.4e9 cells per
 step -- synthetic seeded atoms (pyfstat_gb300.synth).  A step is one pass of
-the batched fused path over all templates (prefix kernel, persistent map
-kernel, finalize kernel; one CUDA graph), giving max2F, argmax and FP64
+the batched fused path over all templates (one CUDA graph of five launches:
+repack -> persistent exp map kernel on one branch, prefix -> persistent rect
+map kernel on the other, then finalize), giving max2F, argmax and FP64
 lnBtSG per template.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
