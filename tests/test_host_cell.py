@@ -235,6 +235,47 @@ def test_exp_row_table_column_equals_generic_column(hostcell):
     assert checked > 50000
 
 
+def test_exp_chunk_paths_long_columns(hostcell):
+    """The row-table walk's chunk paths over several 128-row tables per
+    column: clamped chunks (long taus), steady rows after the first window
+    with an atom and after the first window with data (zero atoms at the end
+    of the data, so the first windows of a column hold none), rows sharing a
+    window start (t0 steps below TAtom), and t0 grids that fall back in
+    places (no steady rows there) -- bit-identical to the generic column."""
+    from _helpers import P
+
+    checked = 0
+    for seed in range(12):
+        rng = np.random.default_rng(4400 + seed)
+        TAtom = 1800 if seed % 2 else int(rng.integers(600, 3000))
+        t0_data, A = synth.merged_atoms(seed, int(rng.integers(150, 400)), 2, Tsft=TAtom,
+                                        gap_frac=0.2)
+        A = A.copy()
+        A[-int(rng.integers(1, 40)):] = 0  # no data at the end
+        n = A.shape[0]
+        nt0 = int(rng.integers(300, 700))
+        span = n * TAtom
+        step = max(1, int(span / nt0 * rng.uniform(0.3, 1.2)))
+        t0s = t0_data + np.arange(nt0, dtype=np.int64) * step
+        if seed % 3 == 0:  # a stretch that falls back by a few steps
+            k = int(rng.integers(50, nt0 - 50))
+            t0s[k:k + 20] -= 3 * step
+        t0s = np.clip(t0s, t0_data, t0_data + span).astype(np.uint32)
+        taus = np.unique(np.round(TAtom * np.logspace(0, np.log10(3 * n), 24))).astype(np.uint32)
+        out = []
+        for comp in (1, 2):
+            F = np.empty((nt0, taus.size), np.float32)
+            hostcell.hc_exp_map(A.ctypes.data_as(P), ctypes.c_uint32(n), ctypes.c_uint32(TAtom),
+                                ctypes.c_uint32(t0_data), t0s.ctypes.data_as(P),
+                                ctypes.c_uint32(nt0), taus.ctypes.data_as(P),
+                                ctypes.c_uint32(taus.size), ctypes.c_int(comp), ctypes.c_uint32(0),
+                                F.ctypes.data_as(P), None)
+            out.append(F)
+        assert np.array_equal(out[0].view(np.uint32), out[1].view(np.uint32)), seed
+        checked += out[0].size
+    assert checked > 50000
+
+
 def test_exp_real_tau_window_sums_match_fp64(hostcell):
     """The forward pass of the differentiable statistics: double-word window
     sums on a real tau grid (window ends from the split 3 tau + TAtom/2 =
