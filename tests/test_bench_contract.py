@@ -85,3 +85,28 @@ def test_gpu_single_template_case_line():
         assert d["case"] == case and d["N_t0"] == 8192 and d["N_tau"] == 4096
         assert d["ms_per_call"] > 0 and d["map_bytes"] == 4.0 * 8192 * 4096
         assert d["map_write_gbs"] == pytest.approx(d["map_bytes"] / d["ms_per_call"] / 1e6)
+
+
+def test_rect_reused_fraction():
+    """The bench line's share of rect cells whose window end equals their
+    left neighbour's: a template whose taus all reach past the data repeats
+    the last atom as every window end after the first column, and one with
+    a tau step of whole SFTs inside the data repeats none."""
+    import numpy as np
+
+    sys.path.insert(0, REPO)
+    import bench
+    from pyfstat_gb300 import _lib
+
+    T, n = 1800, 100
+    desc = np.zeros(2, dtype=_lib.DESC_DTYPE)
+    t0d = 700000000
+    t0s = np.concatenate([t0d + T * np.arange(10), t0d + T * np.arange(10)]).astype(np.uint32)
+    taus = np.concatenate([(n * T + T * np.arange(8)),            # past the data: clamped
+                           (T + T * np.arange(8))]).astype(np.uint32)  # one SFT apart
+    for k in range(2):
+        desc[k] = (0, 10 * k, 8 * k, n, T, t0d, 1, 10, 8)
+    one = bench.rect_reused_fraction(desc[:1], t0s, taus)
+    assert abs(one - 7 / 8) < 1e-12
+    two = bench.rect_reused_fraction(desc[1:], t0s, taus)
+    assert two == 0.0
